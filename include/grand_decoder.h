@@ -1,0 +1,163 @@
+/*
+ * grand_decoder.h -- C ABI of the GB300 GRAND decoder (libgranddecoder.so).
+ *
+ * GRAND (Guessing Random Additive Noise Decoding) over GF(2): for every shot the
+ * decoder finds the lowest-ranked error pattern e of weight <= max_error_weight,
+ * drawn from the shot's active positions, with H.e == s, and reports per-shot
+ * statistics in GrandDecoderResult.
+ *
+ * Drop-in boundary.  The five grand_decode_* functions keep the names, argument
+ * order, argument meaning, struct layouts and return codes of the upstream
+ * library (CarolinaBoavida/Library_S_GRAND, grand_decoder.h:37-176), so an
+ * existing ctypes caller (Examples/auxilary_functions.py:172-253) loads this
+ * library unchanged.  Every search runs on the GPU (sm_103a kernels); there is
+ * no CPU search path.  The search result is the one the upstream CPU search mode
+ * returns (lowest rank in its enumeration order; minimum FP32 LLR cost with its
+ * tie and pruning rules for the ML variant), whatever mode_of_search says;
+ * mode_of_search, threshold_for_hybrid and max_size_active_positions keep their
+ * upstream effect on which threshold iterations are searched and on the
+ * hibrido / total_tested_combinations bookkeeping.
+ *
+ * All matrices are int32, row-major, with entries 0 or 1.  All buffers belong to
+ * the caller.  Functions return 0 on success and a negative value on failure,
+ * with a message on stderr.  Calls are reentrant: no state is shared between
+ * calls except the immutable device binomial table and the code cache, which is
+ * guarded by a mutex.
+ */
+#ifndef GRAND_DECODER_H
+#define GRAND_DECODER_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Largest error weight the search enumerates (upstream grand_decoder.h:28). */
+#define GRAND_MAX_W 6
+
+/* Largest active-position set the GPU search accepts.  Upstream sizes its
+ * binomial table for 300 (grand_decoder.cu:13) and reads past it above that. */
+#define GRAND_MAX_TAM 2048
+
+/* Error codes beyond the upstream -1. */
+#define GRAND_ERR_INVALID   (-1) /* same cases as upstream (bad type, weight, file) */
+#define GRAND_ERR_CUDA      (-2) /* a CUDA call failed; message on stderr            */
+#define GRAND_ERR_LIMIT     (-3) /* a size is beyond what the kernels support        */
+#define GRAND_ERR_CANCELLED (-4) /* a server request was cancelled                   */
+
+/* Upstream grand_decoder.h:37-44 (24 bytes). */
+typedef struct {
+    int max_error_weight;          /* 1..7; searches weights 1..min(w, 6)           */
+    int threads_per_block;         /* accepted for compatibility; tiles are chosen
+                                      by the autotuner                              */
+    int use_gpu_sum;               /* accepted for compatibility; column sums are
+                                      always computed on the GPU                    */
+    int max_size_active_positions; /* cap on the active set (see upstream quirks)   */
+    int threshold_for_hybrid;      /* upstream CPU/GPU switch point (bookkeeping)   */
+    int mode_of_search;            /* -1, 0 or 1 as upstream (bookkeeping + skips)  */
+} GrandDecoderConfig;
+
+/* Upstream grand_decoder.h:53-68 (72 bytes; u64 at offset 24, doubles at 40..64). */
+typedef struct {
+    int found;
+    int found_weight;
+    int original_weight;
+    int degenerate;
+    int is_equal;
+    int tam;
+    unsigned long long total_tested_combinations;
+    int hibrido;
+    int iteration;
+    double time_sum_ms;
+    double total_time_search_ms;
+    double transfer_time_ms;
+    double total_to_find_ms;
+} GrandDecoderResult;
+
+/* ---------------------------------------------------------------------------
+ * The five upstream entry points.
+ * ------------------------------------------------------------------------- */
+
+/* Replaces upstream grand_decode_prob_cc (grand_decoder.h:92, grand_decoder.cu:790).
+ * probability_file holds up to 20 lines "tam_upper o0 o1 o2 p0 p1 p2"; the line
+ * whose tam_upper first covers the active-set size picks the phase order.  A file
+ * with no such line is rejected (upstream reads before its mask array). */
+int grand_decode_prob_cc(const int *Hx, const int *Hz, int n, int m, int *errors,
+                         int *syndromes, int num_shots, const GrandDecoderConfig *config,
+                         GrandDecoderResult *results, char type_of_error,
+                         const char *probability_file);
+
+/* Replaces upstream grand_decode_cc (grand_decoder.h:112, grand_decoder.cu:1117).
+ * errors != NULL: errors (num_shots x m) are the true errors, the syndrome is
+ * H.e and is_equal / degenerate are reported; errors == NULL: syndromes
+ * (num_shots x n) are decoded.  type_of_error 'x'/'X' decodes with Hz, 'z'/'Z'
+ * with Hx. */
+int grand_decode_cc(const int *Hx, const int *Hz, int n, int m, int *errors, int *syndromes,
+                    int num_shots, const GrandDecoderConfig *config,
+                    GrandDecoderResult *results, char type_of_error);
+
+/* Replaces upstream grand_decode_cln (grand_decoder.h:133, grand_decoder.cu:1399).
+ * L_dem is m x n_logicos.  logicals (num_shots x n_logicos) is an INPUT: the
+ * true observable flips; degenerate = 1 when the decoded flips equal them. */
+int grand_decode_cln(int *H_dem, const int *L_dem, int n, int m, int n_logicos,
+                     int *detectors, int *logicals, int num_shots,
+                     const GrandDecoderConfig *config, GrandDecoderResult *results);
+
+/* Replaces upstream grand_decode_prob_cln (grand_decoder.h:154, grand_decoder.cu:1672). */
+int grand_decode_prob_cln(int *H_dem, const int *L_dem, int n, int m, int n_logicos,
+                          int *detectors, int *logicals, int num_shots,
+                          const GrandDecoderConfig *config, GrandDecoderResult *results,
+                          const char *probability_file);
+
+/* Replaces upstream grand_decode_ML_cln (grand_decoder.h:176, grand_decoder.cu:1996).
+ * llr_file holds m FP32 values (one per mechanism).  Non-finite values are
+ * rejected. */
+int grand_decode_ML_cln(int *H_dem, const int *L_dem, int n, int m, int n_logicos,
+                        int *detectors, int *logicals, int num_shots,
+                        const GrandDecoderConfig *config, GrandDecoderResult *results,
+                        const char *llr_file);
+
+/* ---------------------------------------------------------------------------
+ * Extensions (no upstream counterpart): the same five calls, also returning
+ * what upstream computes but never hands back.
+ * ------------------------------------------------------------------------- */
+
+typedef struct {
+    unsigned char *decoded_errors;   /* num_shots x m, 0/1, or NULL                   */
+    unsigned char *decoded_logicals; /* num_shots x n_logicos, 0/1, or NULL (DEM)     */
+    float *ml_cost;                  /* num_shots FP32 LLR cost of the winner, or NULL
+                                        (ML only; 0 when nothing was found)           */
+} GrandDecodeOutputs;
+
+int grand_decode_prob_cc_ex(const int *Hx, const int *Hz, int n, int m, int *errors,
+                            int *syndromes, int num_shots, const GrandDecoderConfig *config,
+                            GrandDecoderResult *results, char type_of_error,
+                            const char *probability_file, const GrandDecodeOutputs *out);
+int grand_decode_cc_ex(const int *Hx, const int *Hz, int n, int m, int *errors, int *syndromes,
+                       int num_shots, const GrandDecoderConfig *config,
+                       GrandDecoderResult *results, char type_of_error,
+                       const GrandDecodeOutputs *out);
+int grand_decode_cln_ex(int *H_dem, const int *L_dem, int n, int m, int n_logicos,
+                        int *detectors, int *logicals, int num_shots,
+                        const GrandDecoderConfig *config, GrandDecoderResult *results,
+                        const GrandDecodeOutputs *out);
+int grand_decode_prob_cln_ex(int *H_dem, const int *L_dem, int n, int m, int n_logicos,
+                             int *detectors, int *logicals, int num_shots,
+                             const GrandDecoderConfig *config, GrandDecoderResult *results,
+                             const char *probability_file, const GrandDecodeOutputs *out);
+int grand_decode_ML_cln_ex(int *H_dem, const int *L_dem, int n, int m, int n_logicos,
+                           int *detectors, int *logicals, int num_shots,
+                           const GrandDecoderConfig *config, GrandDecoderResult *results,
+                           const char *llr_file, const GrandDecodeOutputs *out);
+
+/* Library version string and last error message of the calling thread. */
+const char *grand_version(void);
+const char *grand_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GRAND_DECODER_H */

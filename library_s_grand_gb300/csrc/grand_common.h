@@ -1,0 +1,146 @@
+// grand_common.h -- definitions shared by the host driver and the sm_103a kernels.
+//
+// Layout in HBM (all device-resident, built once per code and cached):
+//   cols   : m columns of H, each packed LSB-first into nwp uint32 words
+//            (nw = ceil(R/32) meaningful words, padded to nwp = 1,2,4,8 or 4k
+//            so a column is one vector load); bit r of column c = H[r][c].
+//   rows   : R rows of H packed into mw = ceil(m/32) words (syndrome of a
+//            supplied error pattern, CSS family).
+//   rref   : reduced row echelon form of the other CSS matrix, rank x mw words,
+//            with its pivot columns (degeneracy test).
+//   lcols  : m rows of L_dem packed into nlw words (DEM logical flips).
+//   llr    : m FP32 LLRs (ML variant).
+//   ncr    : C(n, k) for n <= GRAND_MAX_TAM, k <= 6, as uint64.
+#pragma once
+
+#include <stdint.h>
+
+#include "../../include/grand_decoder.h"
+
+namespace grand {
+
+constexpr int kMaxW = GRAND_MAX_W;        // searched weights 1..6
+constexpr int kMaxTam = GRAND_MAX_TAM;    // largest active set searched
+constexpr int kMaxRows = 1024;            // R <= 1024  -> nw <= 32
+constexpr int kMaxCols = 4096;            // m <= 4096  -> mw <= 128
+constexpr int kMaxLogicals = 1024;
+constexpr int kMaxMasks = 20;             // upstream GRAND_MAX_MASKS (grand_decoder.cu:11)
+constexpr int kMaxIters = 3;              // upstream threshold iterations (grand_decoder.cu:1284)
+constexpr int kMaxSegsPerIter = 15;       // 3 phases x 5 weights
+constexpr int kMaxSegs = kMaxIters * kMaxSegsPerIter;
+
+enum Family { kCss = 0, kDem = 1 };
+enum Variant { kUniform = 0, kProb = 1, kMl = 2 };
+enum InputKind { kInSyndromes = 0, kInErrors = 1, kInDetectors = 2 };
+enum Branch { kBranchGpu = 0, kBranchCpu = 1 };
+
+// Status bits raised by the kernels (read back after every launch).
+enum StatusBits : unsigned {
+  kStatusTamLimit = 1u << 0,      // an active set exceeded GRAND_MAX_TAM
+  kStatusJobOverflow = 1u << 1,   // heavy-job table full: shot deferred
+  kStatusScratchOverflow = 1u << 2,
+  kStatusCasLimit = 1u << 3,      // bounded CAS loop gave up (never expected)
+};
+
+// Immutable per-code tables plus the per-call search parameters.
+struct DevCode {
+  int R, m, nw, nwp, mw;
+  int max_soma, regular;
+  int family, variant, input_kind;
+  int W, Wc;                 // configured weight and min(W, 6)
+  int mode, thr, cap;        // mode_of_search, threshold_for_hybrid, max_size_active_positions
+  int num_phases, n_masks;
+  int mask_tam_upper[kMaxMasks];
+  int mask_order[kMaxMasks][3];
+  int n_logicos, nlw;
+  int rank;                  // rank of RREF(H_other), CSS
+  int rec_len;               // int32 entries per shot record
+  const uint32_t *cols;      // m * nwp
+  const int *colw;           // m
+  const uint32_t *rows;      // R * mw (CSS, errors input)
+  const uint32_t *rref;      // rank * mw
+  const int *piv;            // rank
+  const uint32_t *lcols;     // m * nlw
+  const float *llr;          // m
+};
+
+// One searched weight block of one threshold iteration.
+struct Seg {
+  int iter;                  // index into Job::it
+  int w;                     // weight
+  int dup;                   // weight already listed earlier in this iteration: never matches first
+  int phase;                 // phase position k (prob) or 0
+  unsigned long long base;   // first global candidate index of this block within the shot
+  unsigned long long count;  // C(tam, w)
+  unsigned long long nprefix;// number of (w-1)-prefixes, C(tam-1, w-1)
+  unsigned long long ntiles; // tiles of kLanes x K prefixes
+  unsigned long long chunk_lo; // first chunk of this block within the job
+  unsigned long long nchunks;
+  int K;                     // prefixes per lane in a tile
+};
+
+struct IterInfo {
+  int it;                    // upstream iteration counter value (1-based)
+  int tam;
+  int branch;                // kBranchGpu / kBranchCpu bookkeeping
+  int seg_lo, seg_hi;
+  int src;                   // which threshold mask the active set comes from
+  unsigned long long total;  // full candidate count of the iteration
+  unsigned long long base;   // first global index of the iteration
+  unsigned long long phase_end[3]; // prob: cumulative full count through phase k
+  float prefix[kMaxW + 1];   // ML: FP32 sums of the w smallest LLRs
+  uint32_t *cols;            // tam * nwp staged columns (scratch)
+  int *pos;                  // tam H-column indices (sorted by LLR for ML)
+  float *llr;                // tam LLRs in the same order (ML)
+};
+
+// A shot whose search space is too large for one warp: searched by every
+// block of the persistent search kernel, chunk by chunk.  16-byte aligned: the
+// ML minima are updated with 128-bit compare-and-swap.
+struct alignas(16) Job {
+  int shot, code;
+  int n_it;
+  int nseg;
+  int final_iteration, final_tam, hib_before; // outcome fields if nothing is found
+  unsigned long long chunk_base;  // first global chunk
+  unsigned long long nchunks;
+  unsigned long long best;        // lowest matching global index (atomicMin)
+  unsigned long long chunks_done;
+  int original_weight;
+  int failed;                     // an active set exceeded the kernel limits
+  uint32_t *ebits;                // mw words: supplied error (CSS) / truth logicals (DEM)
+  uint32_t sw[kMaxRows / 32];     // syndrome bits
+  IterInfo it[kMaxIters];
+  Seg seg[kMaxSegs];
+  alignas(16) unsigned long long mlkey[kMaxIters][kMaxW + 1][2]; // ML: {cost key, lex rank} minima
+};
+static_assert(sizeof(Job) % 16 == 0, "Job must keep 16-byte alignment in arrays");
+
+// Everything one batched launch needs.
+struct DevBatch {
+  int num_shots;
+  int num_codes;
+  const DevCode *codes;          // device array
+  const int *in;                 // int32 shot records
+  const long long *in_off;       // per-shot offset into in (nullptr: shot * rec_len of code 0)
+  const int *in_log;             // DEM truth logicals, n_logicos per shot (nullptr: they
+                                 // follow the detector entries inside the record)
+  const int *shot_code;          // per-shot code index (nullptr: code 0)
+  const int *shot_map;           // launch slot -> shot index (nullptr: identity)
+  GrandDecoderResult *results;
+  unsigned char *dec_err;        // num_shots x m (single-code calls) or nullptr
+  unsigned char *dec_log;        // num_shots x n_logicos or nullptr
+  float *ml_cost;                // num_shots or nullptr
+  const unsigned long long *ncr; // (kMaxTam + 1) x (kMaxW + 1)
+  Job *jobs;
+  int max_jobs;
+  unsigned long long *counters;  // [0] packed job/chunk append, [1] next chunk, [2] scratch top
+  uint32_t *scratch;
+  unsigned long long scratch_words;
+  unsigned *status;
+  int *deferred;                 // per shot: 1 if the shot must be re-run
+  int light_max_log2;            // light-path budget (candidates, log2)
+  int tile_k;                    // prefixes per lane per tile for weights >= 3
+};
+
+}  // namespace grand

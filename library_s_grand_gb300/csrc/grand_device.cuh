@@ -1,0 +1,306 @@
+// grand_device.cuh -- device building blocks of the GRAND search (sm_103a).
+//
+// Enumeration.  Upstream enumerates the weight-w subsets of the active positions
+// in lexicographic order of ascending index tuples (grand_decoder.cu:83-100,
+// 264-280) and its CPU mode returns the lowest-ranked match.  Here a weight-w
+// candidate is split into a (w-1)-prefix and a last index j > prefix max.  The
+// prefixes are dealt out in colex order, one prefix per lane, so the 32 lanes of
+// a warp usually share the same prefix maximum; the warp then walks j in
+// lockstep and every lane reads the same staged column (a shared-memory
+// broadcast).  Per candidate a lane does one XOR-OR chain over the column words
+// against T = s ^ (XOR of the prefix columns) and one min: T is updated
+// incrementally when the prefix advances, never recomputed per candidate.
+// Matches are mapped back to their lexicographic rank, so the reduction is an
+// exact minimum over the rank upstream would have reached first, whatever order
+// the tiles run in.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "grand_common.h"
+
+namespace grand {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr unsigned long long kNone = ~0ull;
+
+__device__ __forceinline__ unsigned long long ncr(const unsigned long long *t, int n, int k) {
+  if (n < 0 || k < 0 || n > kMaxTam || k > kMaxW) return 0ull;
+  return __ldg(t + n * (kMaxW + 1) + k);
+}
+
+// Largest v in [lo, hi] with C(v, k) <= q (C(v, k) is non-decreasing in v there).
+__device__ __forceinline__ int ncr_floor(const unsigned long long *t, unsigned long long q, int k,
+                                         int lo, int hi) {
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (ncr(t, mid, k) <= q) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Colex unranking of a k-subset of [0, hi + 1): ascending x[0..k-1].
+__device__ __forceinline__ void colex_unrank(const unsigned long long *t, unsigned long long q,
+                                             int k, int hi, int (&x)[5]) {
+#pragma unroll
+  for (int i = 4; i >= 0; --i) {
+    if (i < k) {
+      int v = ncr_floor(t, q, i + 1, i, hi);
+      q -= ncr(t, v, i + 1);
+      x[i] = v;
+      hi = v - 1;
+    }
+  }
+}
+
+// Lexicographic unranking (upstream order): rank -> ascending c[0..w-1] of [0, n).
+// Computed through the colex rank of the reflected subset {n-1-c}.
+__device__ __forceinline__ void lex_unrank(const unsigned long long *t, unsigned long long rank,
+                                           int n, int w, int (&c)[kMaxW]) {
+  unsigned long long q = ncr(t, n, w) - 1ull - rank;
+  int hi = n - 1;
+#pragma unroll
+  for (int i = kMaxW; i >= 1; --i) {
+    if (i <= w) {
+      int v = ncr_floor(t, q, i, i - 1, hi);
+      q -= ncr(t, v, i);
+      c[w - i] = n - 1 - v;
+      hi = v - 1;
+    }
+  }
+}
+
+// Lexicographic rank of prefix x[0..k-1] followed by last index j (k = w - 1).
+__device__ __forceinline__ unsigned long long lex_rank(const unsigned long long *t, int n, int w,
+                                                       const int (&x)[5], int k, int j) {
+  unsigned long long r = ncr(t, n, w) - 1ull;
+#pragma unroll
+  for (int i = 0; i < 5; ++i)
+    if (i < k) r -= ncr(t, n - 1 - x[i], w - i);
+  r -= (unsigned long long)(n - 1 - j);
+  return r;
+}
+
+// FP32 cost -> unsigned key with the same order (costs are never -0.0: the sum
+// starts from +0.0f, as upstream's does, grand_decoder.cu:641).
+__device__ __forceinline__ uint32_t cost_key(float c) {
+  uint32_t u = __float_as_uint(c);
+  if (c == 0.0f) u = 0u;
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float key_cost(uint32_t k) {
+  uint32_t u = (k & 0x80000000u) ? (k & 0x7fffffffu) : ~k;
+  return __uint_as_float(u);
+}
+
+template <int NW>
+struct Words {
+  static constexpr int nwp = NW <= 2 ? NW : (NW <= 4 ? 4 : 8);
+};
+
+// Column load + mismatch word for compile-time word counts (NW = 1..8); NW = 0
+// is the runtime-width fallback for R > 256.
+template <int NW>
+__device__ __forceinline__ uint32_t mismatch(const uint32_t *col, const uint32_t *T, int nw) {
+  if constexpr (NW == 1) {
+    return col[0] ^ T[0];
+  } else if constexpr (NW == 2) {
+    uint2 a = *reinterpret_cast<const uint2 *>(col);
+    return (a.x ^ T[0]) | (a.y ^ T[1]);
+  } else if constexpr (NW == 3 || NW == 4) {
+    uint4 a = *reinterpret_cast<const uint4 *>(col);
+    uint32_t z = (a.x ^ T[0]) | (a.y ^ T[1]) | (a.z ^ T[2]);
+    if constexpr (NW == 4) z |= a.w ^ T[3];
+    return z;
+  } else if constexpr (NW >= 5 && NW <= 8) {
+    uint4 a = *reinterpret_cast<const uint4 *>(col);
+    uint4 b = *reinterpret_cast<const uint4 *>(col + 4);
+    uint32_t z = (a.x ^ T[0]) | (a.y ^ T[1]) | (a.z ^ T[2]) | (a.w ^ T[3]) | (b.x ^ T[4]);
+    if constexpr (NW >= 6) z |= b.y ^ T[5];
+    if constexpr (NW >= 7) z |= b.z ^ T[6];
+    if constexpr (NW >= 8) z |= b.w ^ T[7];
+    return z;
+  } else {
+    uint32_t z = 0;
+    for (int i = 0; i < nw; ++i) z |= col[i] ^ T[i];
+    return z;
+  }
+}
+
+template <int NW>
+__device__ __forceinline__ void xor_col(uint32_t *T, const uint32_t *col, int nw) {
+  if constexpr (NW >= 1) {
+#pragma unroll
+    for (int i = 0; i < NW; ++i) T[i] ^= col[i];
+  } else {
+    for (int i = 0; i < nw; ++i) T[i] ^= col[i];
+  }
+}
+
+// What one tile evaluation needs to know about its weight block.
+struct SegView {
+  const uint32_t *cols;   // tam x nwp staged active columns
+  const float *llr;       // tam LLRs in the same order (ML)
+  int tam, w, K, nwp, nw;
+  unsigned long long nprefix;
+  unsigned long long base;  // global index of rank 0 (first-hit)
+};
+
+struct LaneBest {
+  unsigned long long g;     // first-hit: lowest global index
+  uint32_t o;               // ML: lowest cost key
+  unsigned long long r;     // ML: its lexicographic rank
+  __device__ __forceinline__ void reset() { g = kNone; o = 0xffffffffu; r = kNone; }
+};
+
+// Evaluate one tile: lane l takes the K colex prefixes tile*32K + l*K + [0, K).
+template <int NW, bool ML>
+__device__ __forceinline__ void eval_tile(const SegView &sv, const unsigned long long *t,
+                                       const uint32_t *sw, unsigned long long tile, LaneBest &lb) {
+  constexpr int NWA = NW ? NW : 32;
+  const int lane = threadIdx.x & 31;
+  const int k = sv.w - 1;
+  const int tam = sv.tam;
+  const int nwp = NW ? Words<NW>::nwp : sv.nwp;
+  const int nw = NW ? NW : sv.nw;
+  const uint32_t *cols = sv.cols;
+
+  unsigned long long q = tile * (32ull * (unsigned long long)sv.K) + (unsigned long long)lane * sv.K;
+  bool valid = q < sv.nprefix;
+  int x[5] = {0, 0, 0, 0, 0};
+  uint32_t T[NWA];
+#pragma unroll
+  for (int i = 0; i < NWA; ++i) T[i] = (i < nw) ? sw[i] : 0u;
+  int clast = -1;
+  if (valid && k > 0) {
+    colex_unrank(t, q, k, tam - 2, x);
+#pragma unroll
+    for (int i = 0; i < 5; ++i)
+      if (i < k) {
+        xor_col<NW>(T, cols + (size_t)x[i] * nwp, nw);
+        clast = x[i];
+      }
+  }
+
+  for (int step = 0; step < sv.K; ++step) {
+    const bool v = valid && (q + step < sv.nprefix);
+    const int cl = v ? clast : tam;
+    const int lo = (int)__reduce_min_sync(kFull, (unsigned)(cl + 1));
+    const int hi = (int)__reduce_max_sync(kFull, v ? (unsigned)(cl + 1) : 0u) - 1;
+    uint32_t acc = 0xffffffffu;
+    int j = lo;
+    const int ahi = hi < tam - 1 ? hi : tam - 1;
+    for (; j <= ahi; ++j) {
+      uint32_t z = mismatch<NW>(cols + (size_t)j * nwp, T, nw);
+      if (j > cl) acc = min(acc, z);
+    }
+    if (j < hi + 1) j = hi + 1;
+#pragma unroll 4
+    for (; j < tam; ++j) acc = min(acc, mismatch<NW>(cols + (size_t)j * nwp, T, nw));
+
+    if (v && acc == 0u) {
+      // A match exists for this prefix: locate it (rare path).
+      for (int jj = cl + 1; jj < tam; ++jj) {
+        if (mismatch<NW>(cols + (size_t)jj * nwp, T, nw) != 0u) continue;
+        unsigned long long r = lex_rank(t, tam, sv.w, x, k, jj);
+        if constexpr (!ML) {
+          unsigned long long g = sv.base + r;
+          if (g < lb.g) lb.g = g;
+          break;
+        } else {
+          float c = 0.0f;
+#pragma unroll
+          for (int i = 0; i < 5; ++i)
+            if (i < k) c = __fadd_rn(c, sv.llr[x[i]]);
+          c = __fadd_rn(c, sv.llr[jj]);
+          uint32_t o = cost_key(c);
+          if (o < lb.o || (o == lb.o && r < lb.r)) {
+            lb.o = o;
+            lb.r = r;
+          }
+        }
+      }
+    }
+
+    if (step + 1 < sv.K && v && k > 0) {
+      // Colex successor: raise the lowest element that has room, reset those below.
+      int adv = -1;
+#pragma unroll
+      for (int i = 0; i < 5; ++i) {
+        if (i < k && adv < 0) {
+          int lim = tam - 1;
+          if (i + 1 < 5 && i + 1 < k) lim = x[(i + 1) < 5 ? i + 1 : 4];
+          if (x[i] + 1 < lim) adv = i;
+        }
+      }
+      if (adv < 0) {
+        valid = false;
+      } else {
+#pragma unroll
+        for (int i = 0; i < 5; ++i) {
+          if (i < k && i <= adv) {
+            int old = x[i];
+            int nv = (i == adv) ? old + 1 : i;
+            if (nv != old) {
+              xor_col<NW>(T, cols + (size_t)old * nwp, nw);
+              xor_col<NW>(T, cols + (size_t)nv * nwp, nw);
+              x[i] = nv;
+            }
+          }
+        }
+#pragma unroll
+        for (int i = 0; i < 5; ++i)
+          if (i < k) clast = x[i];
+      }
+    }
+  }
+}
+
+__device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    unsigned long long u = __shfl_xor_sync(kFull, v, o);
+    v = u < v ? u : v;
+  }
+  return v;
+}
+
+__device__ __forceinline__ void warp_min_key(uint32_t &o, unsigned long long &r) {
+#pragma unroll
+  for (int s = 16; s > 0; s >>= 1) {
+    uint32_t o2 = __shfl_xor_sync(kFull, o, s);
+    unsigned long long r2 = __shfl_xor_sync(kFull, r, s);
+    if (o2 < o || (o2 == o && r2 < r)) {
+      o = o2;
+      r = r2;
+    }
+  }
+}
+
+// 128-bit compare-and-swap minimum of {cost key, rank} (lexicographic).
+__device__ __forceinline__ bool atomic_min_key(unsigned long long *slot, uint32_t o,
+                                               unsigned long long r) {
+  unsigned long long cur0 = *reinterpret_cast<volatile unsigned long long *>(slot);
+  unsigned long long cur1 = *reinterpret_cast<volatile unsigned long long *>(slot + 1);
+  for (int guard = 0; guard < (1 << 20); ++guard) {
+    if ((unsigned long long)o > cur0 || ((unsigned long long)o == cur0 && r >= cur1)) return true;
+    unsigned long long got0, got1;
+    asm volatile(
+        "{\n\t.reg .b128 d, c, n;\n\t"
+        "mov.b128 c, {%2, %3};\n\t"
+        "mov.b128 n, {%4, %5};\n\t"
+        "atom.global.cas.b128 d, [%6], c, n;\n\t"
+        "mov.b128 {%0, %1}, d;\n\t}"
+        : "=l"(got0), "=l"(got1)
+        : "l"(cur0), "l"(cur1), "l"((unsigned long long)o), "l"(r), "l"(slot)
+        : "memory");
+    if (got0 == cur0 && got1 == cur1) return true;
+    cur0 = got0;
+    cur1 = got1;
+  }
+  return false;
+}
+
+}  // namespace grand

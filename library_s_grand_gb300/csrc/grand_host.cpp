@@ -1,0 +1,460 @@
+// grand_host.cpp -- device context, code tables, workspaces and the batch driver.
+#include "grand_host.h"
+
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+
+namespace grand {
+
+static thread_local char g_err[512];
+
+void set_error(const char *fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+  fprintf(stderr, "%s\n", g_err);
+}
+
+const char *last_error() { return g_err; }
+
+#define CK(call)                                                                    \
+  do {                                                                              \
+    cudaError_t e_ = (call);                                                        \
+    if (e_ != cudaSuccess) {                                                        \
+      set_error("grand: CUDA error %s at %s:%d (%s)", cudaGetErrorString(e_), __FILE__, \
+                __LINE__, #call);                                                   \
+      return GRAND_ERR_CUDA;                                                        \
+    }                                                                               \
+  } while (0)
+
+Tuning &tuning() {
+  static Tuning t = [] {
+    Tuning x;
+    if (const char *s = getenv("GRAND_LIGHT_LOG2")) x.light_max_log2 = std::max(0, std::min(40, atoi(s)));
+    if (const char *s = getenv("GRAND_TILE_K")) x.tile_k = std::max(1, std::min(64, atoi(s)));
+    if (const char *s = getenv("GRAND_SEARCH_GRID_MULT")) x.search_grid_mult = std::max(0, atoi(s));
+    return x;
+  }();
+  return t;
+}
+
+cudaError_t ensure(void **p, size_t *cap, size_t bytes) {
+  if (bytes == 0) bytes = 16;
+  if (*p && *cap >= bytes) return cudaSuccess;
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  *cap = 0;
+  size_t want = std::max(bytes, *cap + *cap / 2);
+  cudaError_t e = cudaMalloc(p, want);
+  if (e == cudaSuccess) *cap = want;
+  else *p = nullptr;
+  return e;
+}
+
+CodeTables::~CodeTables() {
+  cudaFree(cols);
+  cudaFree(colw);
+  cudaFree(rref);
+  cudaFree(piv);
+  cudaFree(lcols);
+}
+
+Workspace::~Workspace() {
+  void *bufs[] = {d_in, d_in2, d_res, d_dec, d_declog, d_cost, d_jobs, d_scratch, d_small,
+                  d_deferred, d_map, d_codes, d_llr, d_off, d_shotcode};
+  for (void *b : bufs) cudaFree(b);
+  for (auto &e : ev) if (e) cudaEventDestroy(e);
+  if (stream) cudaStreamDestroy(stream);
+}
+
+static int words_padded(int nw) {
+  if (nw <= 2) return nw;
+  if (nw <= 4) return 4;
+  if (nw <= 8) return 8;
+  return (nw + 3) & ~3;
+}
+
+// Binomials exactly as upstream's multiplicative nCr (grand_decoder.cu:42-52).
+static unsigned long long ncr_host(int n, int k) {
+  if (k < 0 || k > n) return 0;
+  if (k == 0 || k == n) return 1;
+  unsigned long long r = 1;
+  for (int i = 1; i <= k; ++i) r = r * (unsigned long long)(n - i + 1) / (unsigned long long)i;
+  return r;
+}
+
+Context *Context::get(int *err) {
+  static std::mutex mu;
+  static Context *ctxs[64] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) {
+    set_error("grand: no CUDA device available (%s)", cudaGetErrorString(e));
+    *err = GRAND_ERR_CUDA;
+    return nullptr;
+  }
+  std::lock_guard<std::mutex> lk(mu);
+  if (dev < 0 || dev >= 64) {
+    *err = GRAND_ERR_CUDA;
+    return nullptr;
+  }
+  if (ctxs[dev]) return ctxs[dev];
+  cudaDeviceProp prop;
+  e = cudaGetDeviceProperties(&prop, dev);
+  if (e != cudaSuccess) {
+    set_error("grand: cudaGetDeviceProperties failed (%s)", cudaGetErrorString(e));
+    *err = GRAND_ERR_CUDA;
+    return nullptr;
+  }
+  if (prop.major != 10 || prop.minor != 3) {
+    set_error("grand: this library is built for sm_103a (GB300); device %d is sm_%d%d", dev,
+              prop.major, prop.minor);
+    *err = GRAND_ERR_CUDA;
+    return nullptr;
+  }
+  Context *c = new Context();
+  c->device = dev;
+  c->sm_count = prop.multiProcessorCount;
+  int pa = 0;
+  cudaDeviceGetAttribute(&pa, cudaDevAttrPageableMemoryAccess, dev);
+  c->pageable_access = pa;
+  if (occupancy(&c->triage_bps, &c->search_bps) != cudaSuccess) {
+    c->triage_bps = 4;
+    c->search_bps = 2;
+  }
+  std::vector<unsigned long long> t((size_t)(kMaxTam + 1) * (kMaxW + 1));
+  for (int n = 0; n <= kMaxTam; ++n)
+    for (int k = 0; k <= kMaxW; ++k) t[(size_t)n * (kMaxW + 1) + k] = ncr_host(n, k);
+  if (cudaMalloc(&c->d_ncr, t.size() * 8) != cudaSuccess ||
+      cudaMemcpy(c->d_ncr, t.data(), t.size() * 8, cudaMemcpyHostToDevice) != cudaSuccess) {
+    set_error("grand: could not upload the binomial table");
+    *err = GRAND_ERR_CUDA;
+    delete c;
+    return nullptr;
+  }
+  ctxs[dev] = c;
+  return c;
+}
+
+Workspace *Context::acquire() {
+  {
+    std::lock_guard<std::mutex> lk(mu_);
+    if (!pool_.empty()) {
+      Workspace *w = pool_.back();
+      pool_.pop_back();
+      return w;
+    }
+  }
+  Workspace *w = new Workspace();
+  if (cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete w;
+    return nullptr;
+  }
+  for (auto &e : w->ev)
+    if (cudaEventCreate(&e) != cudaSuccess) {
+      delete w;
+      return nullptr;
+    }
+  return w;
+}
+
+void Context::release(Workspace *w) {
+  if (!w) return;
+  std::lock_guard<std::mutex> lk(mu_);
+  pool_.push_back(w);
+}
+
+// GF(2) reduced row echelon form of bit 0 of each entry (grand_decoder.cu:418-454).
+static int rref_bits(std::vector<uint32_t> &rows, int n, int mw, int m, std::vector<int> &piv) {
+  int r = 0;
+  for (int c = 0; c < m && r < n; ++c) {
+    const int q = c >> 5;
+    const uint32_t bit = 1u << (c & 31);
+    int p = -1;
+    for (int i = r; i < n; ++i)
+      if (rows[(size_t)i * mw + q] & bit) { p = i; break; }
+    if (p < 0) continue;
+    if (p != r)
+      for (int j = 0; j < mw; ++j) std::swap(rows[(size_t)r * mw + j], rows[(size_t)p * mw + j]);
+    for (int i = 0; i < n; ++i) {
+      if (i == r || !(rows[(size_t)i * mw + q] & bit)) continue;
+      for (int j = 0; j < mw; ++j) rows[(size_t)i * mw + j] ^= rows[(size_t)r * mw + j];
+    }
+    piv.push_back(c);
+    ++r;
+  }
+  return r;
+}
+
+template <class T>
+static cudaError_t upload(T **d, const std::vector<T> &h) {
+  size_t bytes = std::max<size_t>(h.size() * sizeof(T), 16);
+  cudaError_t e = cudaMalloc(d, bytes);
+  if (e != cudaSuccess) return e;
+  if (h.empty()) return cudaMemset(*d, 0, bytes);
+  return cudaMemcpy(*d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice);
+}
+
+std::shared_ptr<CodeTables> Context::tables(int family, const int *H, const int *H_other,
+                                            const int *L, int n, int m, int nl, int *err) {
+  std::vector<int> key;
+  const size_t nm = (size_t)n * m;
+  key.reserve(6 + nm * (family == kCss ? 2 : 1) + (size_t)m * nl);
+  key.push_back(family);
+  key.push_back(n);
+  key.push_back(m);
+  key.push_back(nl);
+  key.insert(key.end(), H, H + nm);
+  if (family == kCss) key.insert(key.end(), H_other, H_other + nm);
+  else if (nl > 0) key.insert(key.end(), L, L + (size_t)m * nl);
+  {
+    std::lock_guard<std::mutex> lk(mu_);
+    for (size_t i = 0; i < cache_.size(); ++i)
+      if (cache_[i]->key == key) {
+        auto t = cache_[i];
+        cache_.erase(cache_.begin() + i);
+        cache_.push_back(t);
+        return t;
+      }
+  }
+  auto t = std::make_shared<CodeTables>();
+  t->family = family;
+  t->R = n;
+  t->m = m;
+  t->nw = (n + 31) / 32;
+  t->nwp = words_padded(t->nw);
+  t->mw = (m + 31) / 32;
+  t->n_logicos = nl;
+  t->nlw = (nl + 31) / 32;
+  // columns packed LSB-first; statistics on the raw entries (grand_decoder.cu:376-404)
+  std::vector<uint32_t> cols((size_t)m * t->nwp, 0u);
+  std::vector<int> colw(m, 0);
+  for (int r = 0; r < n; ++r)
+    for (int c = 0; c < m; ++c) {
+      const int v = H[(size_t)r * m + c];
+      colw[c] += v;
+      if (v != 0) cols[(size_t)c * t->nwp + (r >> 5)] |= 1u << (r & 31);
+    }
+  t->max_soma = 0;
+  for (int c = 0; c < m; ++c) t->max_soma = std::max(t->max_soma, colw[c]);
+  t->regular = 1;
+  for (int c = 1; c < m; ++c)
+    if (colw[c] != colw[0]) { t->regular = 0; break; }
+  cudaError_t e = upload(&t->cols, cols);
+  if (e == cudaSuccess) e = upload(&t->colw, colw);
+  if (e == cudaSuccess && family == kCss) {
+    std::vector<uint32_t> rows((size_t)n * t->mw, 0u);
+    for (int r = 0; r < n; ++r)
+      for (int c = 0; c < m; ++c)
+        if (H_other[(size_t)r * m + c] & 1) rows[(size_t)r * t->mw + (c >> 5)] |= 1u << (c & 31);
+    std::vector<int> piv;
+    t->rank = rref_bits(rows, n, t->mw, m, piv);
+    rows.resize((size_t)t->rank * t->mw);
+    e = upload(&t->rref, rows);
+    if (e == cudaSuccess) e = upload(&t->piv, piv);
+  }
+  if (e == cudaSuccess && family == kDem) {
+    std::vector<uint32_t> lc((size_t)m * std::max(t->nlw, 1), 0u);
+    for (int c = 0; c < m; ++c)
+      for (int j = 0; j < nl; ++j)
+        if (L[(size_t)c * nl + j] != 0) lc[(size_t)c * t->nlw + (j >> 5)] |= 1u << (j & 31);
+    e = upload(&t->lcols, lc);
+  }
+  if (e != cudaSuccess) {
+    set_error("grand: could not upload code tables (%s)", cudaGetErrorString(e));
+    *err = GRAND_ERR_CUDA;
+    return nullptr;
+  }
+  t->bytes = cols.size() * 4 + colw.size() * 4 + key.size() * 4;
+  t->key.swap(key);
+  std::lock_guard<std::mutex> lk(mu_);
+  cache_.push_back(t);
+  cache_bytes_ += t->bytes;
+  while (cache_.size() > 64 || (cache_bytes_ > (512u << 20) && cache_.size() > 1)) {
+    cache_bytes_ -= cache_.front()->bytes;
+    cache_.erase(cache_.begin());
+  }
+  return t;
+}
+
+DevCode make_devcode(const CodeTables &t, const CallParams &p) {
+  DevCode d;
+  memset(&d, 0, sizeof(d));
+  d.R = t.R;
+  d.m = t.m;
+  d.nw = t.nw;
+  d.nwp = t.nwp;
+  d.mw = t.mw;
+  d.max_soma = t.max_soma;
+  d.regular = t.regular;
+  d.family = t.family;
+  d.variant = p.variant;
+  d.input_kind = p.input_kind;
+  d.W = p.W;
+  d.Wc = std::min(p.W, (int)kMaxW);
+  d.mode = p.mode;
+  d.thr = p.thr;
+  d.cap = p.cap;
+  d.num_phases = p.num_phases;
+  d.n_masks = p.n_masks;
+  memcpy(d.mask_tam_upper, p.mask_tam_upper, sizeof(d.mask_tam_upper));
+  memcpy(d.mask_order, p.mask_order, sizeof(d.mask_order));
+  d.n_logicos = t.n_logicos;
+  d.nlw = t.nlw;
+  d.rank = t.rank;
+  d.rec_len = p.input_kind == kInErrors ? t.m : t.R;
+  d.cols = t.cols;
+  d.colw = t.colw;
+  d.rows = nullptr;
+  d.rref = t.rref;
+  d.piv = t.piv;
+  d.lcols = t.lcols;
+  d.llr = p.d_llr;
+  return d;
+}
+
+int run_batch(Context *ctx, Workspace *ws, const BatchRequest &req, BatchTiming *timing) {
+  const int N = req.num_shots;
+  if (N <= 0) return 0;
+  cudaStream_t s = ws->stream;
+  const Tuning &tn = tuning();
+  const int ncodes = (int)req.codes.size();
+
+  CK(ensure(&ws->d_codes, &ws->cap_codes, sizeof(DevCode) * ncodes));
+  CK(ensure(&ws->d_in, &ws->cap_in, req.in_ints * sizeof(int)));
+  if (req.h_in_log) CK(ensure(&ws->d_in2, &ws->cap_in2, req.in_log_ints * sizeof(int)));
+  if (req.h_off) CK(ensure(&ws->d_off, &ws->cap_off, sizeof(long long) * N));
+  if (req.h_shot_code) CK(ensure(&ws->d_shotcode, &ws->cap_shotcode, sizeof(int) * N));
+  CK(ensure(&ws->d_res, &ws->cap_res, sizeof(GrandDecoderResult) * N));
+  if (req.h_dec_err) CK(ensure(&ws->d_dec, &ws->cap_dec, (size_t)N * req.dec_m));
+  if (req.h_dec_log) CK(ensure(&ws->d_declog, &ws->cap_declog, (size_t)N * std::max(req.dec_nl, 1)));
+  if (req.h_cost) CK(ensure(&ws->d_cost, &ws->cap_cost, sizeof(float) * N));
+  const int max_jobs = std::min(N, 16384);
+  CK(ensure(&ws->d_jobs, &ws->cap_jobs, sizeof(Job) * max_jobs));
+  const size_t scratch_words = 32ull << 20;
+  CK(ensure(&ws->d_scratch, &ws->cap_scratch, scratch_words * 4));
+  size_t small_cap = ws->d_small ? 256 : 0;
+  CK(ensure(&ws->d_small, &small_cap, 256));
+  CK(ensure(&ws->d_deferred, &ws->cap_deferred, sizeof(int) * N));
+
+  CK(cudaEventRecord(ws->ev[0], s));
+  CK(cudaMemcpyAsync(ws->d_codes, req.codes.data(), sizeof(DevCode) * ncodes,
+                     cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(ws->d_in, req.h_in, req.in_ints * sizeof(int), cudaMemcpyHostToDevice, s));
+  if (req.h_in_log)
+    CK(cudaMemcpyAsync(ws->d_in2, req.h_in_log, req.in_log_ints * sizeof(int),
+                       cudaMemcpyHostToDevice, s));
+  if (req.h_off)
+    CK(cudaMemcpyAsync(ws->d_off, req.h_off, sizeof(long long) * N, cudaMemcpyHostToDevice, s));
+  if (req.h_shot_code)
+    CK(cudaMemcpyAsync(ws->d_shotcode, req.h_shot_code, sizeof(int) * N, cudaMemcpyHostToDevice, s));
+  CK(cudaEventRecord(ws->ev[1], s));
+
+  DevBatch b;
+  memset(&b, 0, sizeof(b));
+  b.num_codes = ncodes;
+  b.codes = (const DevCode *)ws->d_codes;
+  b.in = (const int *)ws->d_in;
+  b.in_off = req.h_off ? (const long long *)ws->d_off : nullptr;
+  b.in_log = req.h_in_log ? (const int *)ws->d_in2 : nullptr;
+  b.shot_code = req.h_shot_code ? (const int *)ws->d_shotcode : nullptr;
+  b.results = (GrandDecoderResult *)ws->d_res;
+  b.dec_err = req.h_dec_err ? (unsigned char *)ws->d_dec : nullptr;
+  b.dec_log = req.h_dec_log ? (unsigned char *)ws->d_declog : nullptr;
+  b.ml_cost = req.h_cost ? (float *)ws->d_cost : nullptr;
+  b.ncr = ctx->d_ncr;
+  b.jobs = (Job *)ws->d_jobs;
+  b.max_jobs = max_jobs;
+  b.counters = (unsigned long long *)ws->d_small;
+  b.status = (unsigned *)((char *)ws->d_small + 128);
+  b.scratch = (uint32_t *)ws->d_scratch;
+  b.scratch_words = scratch_words;
+  b.deferred = (int *)ws->d_deferred;
+  b.light_max_log2 = tn.light_max_log2;
+  b.tile_k = tn.tile_k;
+
+  const int tgrid_max = ctx->sm_count * std::max(ctx->triage_bps, 1);
+  const int sgrid = ctx->sm_count * std::max(1, tn.search_grid_mult ? tn.search_grid_mult : ctx->search_bps);
+  std::vector<int> map;
+  int todo = N;
+  float tri_ms = 0, sea_ms = 0;
+  int rounds = 0;
+  unsigned status_all = 0;
+  for (;;) {
+    b.num_shots = todo;
+    b.shot_map = rounds == 0 ? nullptr : (const int *)ws->d_map;
+    CK(cudaMemsetAsync(ws->d_small, 0, 256, s));
+    const int twarps = 4;
+    const int tgrid = std::max(1, std::min(tgrid_max, (todo + twarps - 1) / twarps));
+    CK(cudaEventRecord(ws->ev[2], s));
+    CK(launch_triage(b, tgrid, s));
+    CK(cudaEventRecord(ws->ev[3], s));
+    CK(launch_search(b, sgrid, s));
+    CK(cudaEventRecord(ws->ev[4], s));
+    unsigned st = 0;
+    CK(cudaMemcpyAsync(&st, b.status, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    float a = 0, c = 0;
+    cudaEventElapsedTime(&a, ws->ev[2], ws->ev[3]);
+    cudaEventElapsedTime(&c, ws->ev[3], ws->ev[4]);
+    tri_ms += a;
+    sea_ms += c;
+    ++rounds;
+    status_all |= st;
+    if (!(st & (kStatusJobOverflow | kStatusScratchOverflow))) break;
+    // Re-run the shots that did not fit the job table or scratch.
+    std::vector<int> def(N);
+    CK(cudaMemcpy(def.data(), ws->d_deferred, sizeof(int) * N, cudaMemcpyDeviceToHost));
+    std::vector<int> prev = map;
+    map.clear();
+    if (rounds == 1) {
+      for (int i = 0; i < N; ++i) if (def[i]) map.push_back(i);
+    } else {
+      for (int i : prev) if (def[i]) map.push_back(i);
+    }
+    if (map.empty() || rounds > 64) break;
+    todo = (int)map.size();
+    CK(ensure(&ws->d_map, &ws->cap_map, sizeof(int) * map.size()));
+    CK(cudaMemcpyAsync(ws->d_map, map.data(), sizeof(int) * map.size(), cudaMemcpyHostToDevice, s));
+  }
+
+  CK(cudaEventRecord(ws->ev[4], s));
+  CK(cudaMemcpyAsync(req.h_results, ws->d_res, sizeof(GrandDecoderResult) * N,
+                     cudaMemcpyDeviceToHost, s));
+  if (req.h_dec_err)
+    CK(cudaMemcpyAsync(req.h_dec_err, ws->d_dec, (size_t)N * req.dec_m, cudaMemcpyDeviceToHost, s));
+  if (req.h_dec_log && req.dec_nl > 0)
+    CK(cudaMemcpyAsync(req.h_dec_log, ws->d_declog, (size_t)N * req.dec_nl,
+                       cudaMemcpyDeviceToHost, s));
+  if (req.h_cost)
+    CK(cudaMemcpyAsync(req.h_cost, ws->d_cost, sizeof(float) * N, cudaMemcpyDeviceToHost, s));
+  CK(cudaEventRecord(ws->ev[5], s));
+  CK(cudaStreamSynchronize(s));
+  float h2d = 0, d2h = 0;
+  cudaEventElapsedTime(&h2d, ws->ev[0], ws->ev[1]);
+  cudaEventElapsedTime(&d2h, ws->ev[4], ws->ev[5]);
+  if (timing) {
+    timing->h2d_ms = h2d;
+    timing->triage_ms = tri_ms;
+    timing->search_ms = sea_ms;
+    timing->d2h_ms = d2h;
+    timing->rounds = rounds;
+  }
+  if (status_all & kStatusTamLimit) {
+    set_error("grand: an active-position set exceeded GRAND_MAX_TAM=%d; those shots are "
+              "reported unsearched", kMaxTam);
+    return GRAND_ERR_LIMIT;
+  }
+  if (status_all & kStatusCasLimit) {
+    set_error("grand: internal ML reduction retry limit reached");
+    return GRAND_ERR_CUDA;
+  }
+  return 0;
+}
+
+}  // namespace grand

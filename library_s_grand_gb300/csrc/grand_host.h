@@ -1,0 +1,131 @@
+// grand_host.h -- host-side driver of the GB300 GRAND decoder.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "grand_common.h"
+
+namespace grand {
+
+// Kernel launchers (grand_kernels.cu).
+cudaError_t launch_triage(const DevBatch &b, int grid, cudaStream_t s);
+cudaError_t launch_search(const DevBatch &b, int grid, cudaStream_t s);
+cudaError_t occupancy(int *triage_blocks_per_sm, int *search_blocks_per_sm);
+
+void set_error(const char *fmt, ...);
+
+// Device-resident tables of one matrix set; shared by every call that decodes
+// with the same matrices (cached by content).
+struct CodeTables {
+  int family = 0;
+  int R = 0, m = 0, nw = 0, nwp = 0, mw = 0;
+  int max_soma = 0, regular = 1, rank = 0;
+  int n_logicos = 0, nlw = 0;
+  uint32_t *cols = nullptr;
+  int *colw = nullptr;
+  uint32_t *rref = nullptr;
+  int *piv = nullptr;
+  uint32_t *lcols = nullptr;
+  std::vector<int> key;  // exact content the tables were built from
+  size_t bytes = 0;
+  ~CodeTables();
+};
+
+// Per-call parameters that complete a CodeTables into a DevCode.
+struct CallParams {
+  int variant = kUniform;
+  int input_kind = kInSyndromes;
+  int W = 1;
+  int mode = -1, thr = 0, cap = 0;
+  int num_phases = 0, n_masks = 0;
+  int mask_tam_upper[kMaxMasks] = {};
+  int mask_order[kMaxMasks][3] = {};
+  const float *d_llr = nullptr;   // device LLRs (ML)
+};
+
+DevCode make_devcode(const CodeTables &t, const CallParams &p);
+
+// Growable device/host buffers and a stream, reused across calls.
+struct Workspace {
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[6] = {};
+  void *d_in = nullptr; size_t cap_in = 0;
+  void *d_in2 = nullptr; size_t cap_in2 = 0;
+  void *d_res = nullptr; size_t cap_res = 0;
+  void *d_dec = nullptr; size_t cap_dec = 0;
+  void *d_declog = nullptr; size_t cap_declog = 0;
+  void *d_cost = nullptr; size_t cap_cost = 0;
+  void *d_jobs = nullptr; size_t cap_jobs = 0;
+  void *d_scratch = nullptr; size_t cap_scratch = 0;
+  void *d_small = nullptr;  // counters, status
+  void *d_deferred = nullptr; size_t cap_deferred = 0;
+  void *d_map = nullptr; size_t cap_map = 0;
+  void *d_codes = nullptr; size_t cap_codes = 0;
+  void *d_llr = nullptr; size_t cap_llr = 0;
+  void *d_off = nullptr; size_t cap_off = 0;
+  void *d_shotcode = nullptr; size_t cap_shotcode = 0;
+  ~Workspace();
+};
+
+cudaError_t ensure(void **p, size_t *cap, size_t bytes);
+
+class Context {
+ public:
+  static Context *get(int *err);
+  int device = 0;
+  int sm_count = 0;
+  int triage_bps = 1, search_bps = 1;
+  unsigned long long *d_ncr = nullptr;
+  int pageable_access = 0;
+
+  std::shared_ptr<CodeTables> tables(int family, const int *H, const int *H_other,
+                                     const int *L, int n, int m, int n_logicos, int *err);
+  Workspace *acquire();
+  void release(Workspace *w);
+
+ private:
+  std::mutex mu_;
+  std::vector<std::shared_ptr<CodeTables>> cache_;  // most recent last
+  std::vector<Workspace *> pool_;
+  size_t cache_bytes_ = 0;
+};
+
+// One batched decode of shots that may mix several codes.
+struct BatchRequest {
+  int num_shots = 0;
+  std::vector<DevCode> codes;        // host copies (device pointers inside)
+  const int *h_in = nullptr;         // host int32 records (copied to the device)
+  size_t in_ints = 0;
+  const int *h_in_log = nullptr;     // DEM truth logicals in a separate array
+  size_t in_log_ints = 0;
+  const long long *h_off = nullptr;  // per-shot record offsets (multi-code)
+  const int *h_shot_code = nullptr;
+  GrandDecoderResult *h_results = nullptr;
+  unsigned char *h_dec_err = nullptr;
+  unsigned char *h_dec_log = nullptr;
+  float *h_cost = nullptr;
+  int dec_m = 0, dec_nl = 0;
+};
+
+struct BatchTiming {
+  float h2d_ms = 0, triage_ms = 0, search_ms = 0, d2h_ms = 0;
+  int rounds = 0;
+};
+
+// Runs the batch; returns 0 or a GRAND_ERR_* code.
+int run_batch(Context *ctx, Workspace *ws, const BatchRequest &req, BatchTiming *timing);
+
+// Tunables (environment overrides, autotuner results).
+struct Tuning {
+  int light_max_log2 = 12;
+  int tile_k = 4;
+  int search_grid_mult = 0;  // 0: occupancy-derived
+};
+Tuning &tuning();
+
+}  // namespace grand

@@ -1,0 +1,804 @@
+// grand_kernels.cu -- the two kernels of one decoding launch (sm_103a).
+//
+// triage_kernel (one warp per shot, grid-stride over the batch)
+//   packs the shot's int32 record into bits, forms the syndrome, computes the
+//   flagged-check count of every column (popc(col & s), upstream
+//   grand_decoder.cu:67-81 / 352-374, with the irregular offset of :406-416),
+//   the active sets of the <= 3 threshold iterations (:1284-1290, :495-504),
+//   the upstream active-set cap and mode rules (:1296, :1327, :1550-1554), and
+//   the weight blocks each searched iteration enumerates.  Shots whose whole
+//   search space fits the light budget are searched and finished by the same
+//   warp; the others become Jobs for the persistent search kernel.
+//
+// search_kernel (persistent, one CTA per resident slot)
+//   every CTA repeatedly takes the next chunk (a run of tiles of one weight
+//   block of one Job) from a global counter, stages the block's active columns
+//   in shared memory, lets its 8 warps evaluate the tiles, publishes the lowest
+//   matching global index (atomicMin) or the lowest {cost, rank} key (128-bit
+//   CAS), and the CTA that completes a Job's last chunk writes its result.
+//   Chunks whose candidates all rank above an already-found match are skipped.
+//   No CTA ever waits for another.
+#include <cuda_runtime.h>
+
+#include "grand_device.cuh"
+
+namespace grand {
+
+constexpr int kTriageWarps = 4;
+constexpr int kLightTam = 96;
+constexpr int kLightWords = kLightTam * 8;
+constexpr int kSearchThreads = 256;
+constexpr int kSearchWarps = kSearchThreads / 32;
+constexpr int kStageWords = 8192;
+constexpr int kTilesPerChunk = kSearchWarps;
+
+struct alignas(16) WarpArea {
+  uint32_t cols[kLightWords];
+  float llr[kLightTam];
+  int pos[kLightTam];
+  int tmp[kLightTam];
+  uint32_t sw[kMaxRows / 32];
+  uint32_t eb[kMaxCols / 32];
+  uint32_t am[kMaxIters][kMaxCols / 32];
+  uint32_t delta[kMaxCols / 32];
+  Job job;
+};
+
+// ---------------------------------------------------------------------------
+// Planning: the threshold iterations and their weight blocks (lane 0 only).
+// ---------------------------------------------------------------------------
+__device__ void plan_shot(const DevCode &cd, const unsigned long long *t, const int (&tam_raw)[3],
+                          int L, int tile_k, Job &J) {
+  J.n_it = 0;
+  J.nseg = 0;
+  J.failed = 0;
+  int tam = 0, tam_old = 0, passes = 0;
+  unsigned long long gbase = 0;
+  for (int i = 0; i < L; ++i) {
+    passes = i + 1;
+    tam = tam_raw[i];
+    if (cd.family == kDem) {  // grand_decoder.cu:1550-1554
+      if (tam > cd.cap) tam = tam_old;
+      else tam_old = tam;
+    }
+    if (tam <= 0) continue;
+    const bool gpu = (tam > cd.thr && tam <= cd.cap && cd.mode == 1) || cd.mode == 0;
+    const bool cpu = !gpu && ((tam <= cd.thr && cd.mode == 1) || cd.mode == -1);
+    if (!gpu && !cpu) continue;
+    if (tam > kMaxTam) {
+      J.failed = 1;
+      continue;
+    }
+    IterInfo &I = J.it[J.n_it];
+    I.it = i + 1;
+    I.tam = tam;
+    I.branch = gpu ? kBranchGpu : kBranchCpu;
+    I.src = i;
+    I.seg_lo = J.nseg;
+    I.base = gbase;
+    I.phase_end[0] = I.phase_end[1] = I.phase_end[2] = 0;
+    unsigned long long tot = 0;
+    int wl[kMaxSegsPerIter], ph[kMaxSegsPerIter], nwl = 0;
+    if (cd.variant == kProb) {
+      int mi = cd.n_masks - 1;  // grand_decoder.cu:754-762
+      for (int q = 0; q < cd.n_masks; ++q)
+        if (tam <= cd.mask_tam_upper[q]) { mi = q; break; }
+      for (int k = 0; k < cd.num_phases; ++k) {  // grand_decoder.cu:764-786
+        const int pid = cd.mask_order[mi][k];
+        if (pid == 0) {
+          for (int w = 1; w <= 5 && w <= tam && w <= kMaxW; ++w) { wl[nwl] = w; ph[nwl++] = k; }
+        } else if (pid == 1) {
+          if (6 <= tam && 6 <= kMaxW) { wl[nwl] = 6; ph[nwl++] = k; }
+        }
+      }
+    } else {
+      const int wmax = cd.Wc < tam ? cd.Wc : tam;
+      for (int w = 1; w <= wmax; ++w) { wl[nwl] = w; ph[nwl++] = 0; }
+    }
+    unsigned seen = 0;
+    for (int q = 0; q < nwl; ++q) {
+      Seg &S = J.seg[J.nseg++];
+      S.iter = J.n_it;
+      S.w = wl[q];
+      S.phase = ph[q];
+      S.dup = (seen >> S.w) & 1u;
+      seen |= 1u << S.w;
+      S.count = ncr(t, tam, S.w);
+      S.base = gbase + tot;
+      S.nprefix = ncr(t, tam - 1, S.w - 1);
+      S.K = S.w <= 2 ? 1 : tile_k;
+      S.ntiles = (S.nprefix + 32ull * S.K - 1) / (32ull * S.K);
+      tot += S.count;
+      if (cd.variant == kProb) I.phase_end[S.phase] = tot;
+    }
+    if (cd.variant == kProb)  // phases without weights keep the running total
+      for (int k = 1; k < 3; ++k)
+        if (I.phase_end[k] < I.phase_end[k - 1]) I.phase_end[k] = I.phase_end[k - 1];
+    I.seg_hi = J.nseg;
+    I.total = tot;
+    gbase += tot;
+    J.n_it++;
+  }
+  J.final_iteration = passes;
+  J.final_tam = tam;
+}
+
+// ---------------------------------------------------------------------------
+// Result writer shared by the light path and the search kernel (one warp).
+// ---------------------------------------------------------------------------
+struct Winner {
+  int found;
+  int ii;                   // index into J.it
+  int seg;                  // index into J.seg
+  unsigned long long rank;  // lexicographic rank inside the weight block
+  unsigned long long count; // candidates the winning iteration reports
+  float cost;
+};
+
+__device__ void finish_shot(const DevBatch &b, const DevCode &cd, const Job &J, int shot,
+                            const Winner &wn, const uint32_t *ebits, uint32_t *delta) {
+  const int lane = threadIdx.x & 31;
+  int p[kMaxW];
+  int w = 0;
+  if (wn.found) {
+    const Seg &S = J.seg[wn.seg];
+    const IterInfo &I = J.it[wn.ii];
+    w = S.w;
+    int c[kMaxW];
+    lex_unrank(b.ncr, wn.rank, I.tam, w, c);
+#pragma unroll
+    for (int i = 0; i < kMaxW; ++i) p[i] = (i < w) ? I.pos[c[i]] : -1;
+  } else {
+#pragma unroll
+    for (int i = 0; i < kMaxW; ++i) p[i] = -1;
+  }
+
+  int degenerate = 0, is_equal = 0;
+  if (wn.found && cd.family == kCss && cd.input_kind == kInErrors) {
+    // is_equal: supplied error == decoded error (grand_decoder.cu:1362).
+    bool eq = true;
+    for (int q = lane; q < cd.mw; q += 32) {
+      uint32_t e = 0;
+#pragma unroll
+      for (int i = 0; i < kMaxW; ++i)
+        if (i < w && (p[i] >> 5) == q) e |= 1u << (p[i] & 31);
+      uint32_t d = ebits[q] ^ e;
+      delta[q] = d;
+      eq = eq && d == 0u;
+    }
+    is_equal = __all_sync(kFull, eq) ? 1 : 0;
+    __syncwarp();
+    // degenerate: (e ^ e_est) in the row space of the other matrix
+    // (grand_decoder.cu:456-474).  In reduced row echelon form the pivot bits of
+    // the vector decide alone which rows are added.
+    bool ok = true;
+    for (int q = lane; q < cd.mw; q += 32) {
+      uint32_t acc = 0;
+      for (int r = 0; r < cd.rank; ++r) {
+        const int pc = __ldg(cd.piv + r);
+        if ((delta[pc >> 5] >> (pc & 31)) & 1u) acc ^= __ldg(cd.rref + (size_t)r * cd.mw + q);
+      }
+      ok = ok && acc == delta[q];
+    }
+    degenerate = __all_sync(kFull, ok) ? 1 : 0;
+  } else if (wn.found && cd.family == kDem) {
+    // decoded logical flips vs the supplied true flips (grand_decoder.cu:1623-1644)
+    bool eq = true;
+    for (int q = lane; q < cd.nlw; q += 32) {
+      uint32_t le = 0;
+#pragma unroll
+      for (int i = 0; i < kMaxW; ++i)
+        if (i < w) le ^= __ldg(cd.lcols + (size_t)p[i] * cd.nlw + q);
+      eq = eq && le == ebits[q];
+      if (b.dec_log) {
+        for (int j = 0; j < 32 && q * 32 + j < cd.n_logicos; ++j)
+          b.dec_log[(size_t)shot * cd.n_logicos + q * 32 + j] = (unsigned char)((le >> j) & 1u);
+      }
+    }
+    degenerate = __all_sync(kFull, eq) ? 1 : 0;
+  } else if (cd.family == kDem && b.dec_log) {
+    for (int j = lane; j < cd.n_logicos; j += 32) b.dec_log[(size_t)shot * cd.n_logicos + j] = 0;
+  }
+
+  if (b.dec_err) {
+    for (int c = lane; c < cd.m; c += 32) {
+      unsigned char v = 0;
+#pragma unroll
+      for (int i = 0; i < kMaxW; ++i)
+        if (i < w && p[i] == c) v = 1;
+      b.dec_err[(size_t)shot * cd.m + c] = v;
+    }
+  }
+
+  if (lane == 0) {
+    int h = -2;
+    unsigned long long tested = 0;
+    const int last = wn.found ? wn.ii : J.n_it - 1;
+    for (int k = 0; k <= last; ++k) {
+      h = (J.it[k].branch == kBranchGpu) ? (h == -1 ? 1 : 0) : -1;
+      if (k < last || !wn.found) tested += J.it[k].total;
+    }
+    if (wn.found) tested += wn.count;
+    GrandDecoderResult r;
+    r.found = wn.found;
+    r.found_weight = w;
+    r.original_weight = J.original_weight;
+    r.degenerate = degenerate;
+    r.is_equal = is_equal;
+    r.tam = wn.found ? J.it[wn.ii].tam : J.final_tam;
+    r.total_tested_combinations = tested;
+    r.hibrido = h;
+    r.iteration = wn.found ? J.it[wn.ii].it : J.final_iteration;
+    r.time_sum_ms = 0.0;
+    r.total_time_search_ms = 0.0;
+    r.transfer_time_ms = 0.0;
+    r.total_to_find_ms = 0.0;
+    b.results[shot] = r;
+    if (b.ml_cost) b.ml_cost[shot] = wn.found ? wn.cost : 0.0f;
+    if (J.failed) atomicOr(b.status, kStatusTamLimit);
+  }
+}
+
+// Winner of a first-hit search from the lowest matching global index.
+__device__ Winner winner_from_index(const Job &J, unsigned long long g, bool prob) {
+  Winner wn;
+  wn.found = 0;
+  wn.ii = wn.seg = 0;
+  wn.rank = wn.count = 0;
+  wn.cost = 0.0f;
+  if (g == kNone) return wn;
+  for (int ii = 0; ii < J.n_it; ++ii) {
+    const IterInfo &I = J.it[ii];
+    if (g < I.base || g >= I.base + I.total) continue;
+    for (int s = I.seg_lo; s < I.seg_hi; ++s) {
+      const Seg &S = J.seg[s];
+      if (S.dup || g < S.base || g >= S.base + S.count) continue;
+      wn.found = 1;
+      wn.ii = ii;
+      wn.seg = s;
+      wn.rank = g - S.base;
+      if (I.branch == kBranchCpu) wn.count = g - I.base + 1ull;  // grand_decoder.cu:547-548
+      else if (prob) wn.count = I.phase_end[S.phase];            // grand_decoder.cu:1006
+      else wn.count = I.total;                                   // grand_decoder.cu:1303-1304
+      return wn;
+    }
+  }
+  return wn;
+}
+
+// ---------------------------------------------------------------------------
+// Staging of one iteration's active set (positions, columns, LLRs).
+// ---------------------------------------------------------------------------
+__device__ void stage_iteration(const DevCode &cd, const uint32_t *am, int tam, int *pos,
+                                int *tmp, uint32_t *cols, float *llr) {
+  const int lane = threadIdx.x & 31;
+  const bool ml = cd.variant == kMl;
+  int *dst = ml ? tmp : pos;
+  // ascending column indices of the first tam set bits (upstream extract_positions)
+  int base = 0;
+  for (int q = 0; q < cd.mw && base < tam; ++q) {
+    const uint32_t word = am[q];
+    const bool bit = (word >> lane) & 1u;
+    const int idx = base + __popc(word & ((1u << lane) - 1u));
+    if (bit && idx < tam) dst[idx] = q * 32 + lane;
+    base += __popc(word);
+  }
+  __syncwarp();
+  if (ml) {
+    // stable sort by LLR ascending (upstream insertion sort, grand_decoder.cu:598-610)
+    for (int i = lane; i < tam; i += 32) {
+      const float key = __ldg(cd.llr + tmp[i]);
+      int r = 0;
+      for (int j = 0; j < tam; ++j) {
+        const float kj = __ldg(cd.llr + tmp[j]);
+        r += (kj < key) || (kj == key && j < i);
+      }
+      pos[r] = tmp[i];
+    }
+    __syncwarp();
+  }
+  const int nwp = cd.nwp;
+  for (int idx = lane; idx < tam * nwp; idx += 32) {
+    const int i = idx / nwp;
+    cols[idx] = __ldg(cd.cols + (size_t)pos[i] * nwp + (idx - i * nwp));
+  }
+  if (ml)
+    for (int i = lane; i < tam; i += 32) llr[i] = __ldg(cd.llr + pos[i]);
+  __syncwarp();
+}
+
+// ---------------------------------------------------------------------------
+// Evaluation dispatch on the column word count.
+// ---------------------------------------------------------------------------
+template <bool ML>
+__device__ __forceinline__ void eval_dispatch(int nw, const SegView &sv,
+                                              const unsigned long long *t, const uint32_t *sw,
+                                              unsigned long long tile, LaneBest &lb) {
+  switch (nw) {
+    case 1: eval_tile<1, ML>(sv, t, sw, tile, lb); break;
+    case 2: eval_tile<2, ML>(sv, t, sw, tile, lb); break;
+    case 3: eval_tile<3, ML>(sv, t, sw, tile, lb); break;
+    case 4: eval_tile<4, ML>(sv, t, sw, tile, lb); break;
+    case 5: eval_tile<5, ML>(sv, t, sw, tile, lb); break;
+    case 6: eval_tile<6, ML>(sv, t, sw, tile, lb); break;
+    case 7: eval_tile<7, ML>(sv, t, sw, tile, lb); break;
+    case 8: eval_tile<8, ML>(sv, t, sw, tile, lb); break;
+    default: eval_tile<0, ML>(sv, t, sw, tile, lb); break;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Kernel 1: triage + light search.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
+  __shared__ WarpArea areas[kTriageWarps];
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  WarpArea &A = areas[wib];
+  const int gw = blockIdx.x * kTriageWarps + wib;
+  const int nwarps = gridDim.x * kTriageWarps;
+
+  for (int slot = gw; slot < b.num_shots; slot += nwarps) {
+    const int shot = b.shot_map ? b.shot_map[slot] : slot;
+    const int ci = b.shot_code ? b.shot_code[shot] : 0;
+    const DevCode &cd = b.codes[ci];
+    const int *rec = b.in + (b.in_off ? b.in_off[shot] : (long long)shot * cd.rec_len);
+    Job &J = A.job;
+
+    // ---- pack the record ---------------------------------------------------
+    uint32_t s_lane = 0;  // lane w holds syndrome word w
+    int original_weight = 0;
+    if (cd.input_kind == kInErrors) {
+      for (int q = 0; q < cd.mw; ++q) {
+        const int c = q * 32 + lane;
+        const int v = c < cd.m ? rec[c] : 0;
+        const uint32_t bits = __ballot_sync(kFull, v != 0);
+        if (lane == 0) A.eb[q] = bits;
+        original_weight += __popc(bits);
+      }
+      __syncwarp();
+      // s = XOR of the columns of the supplied error (grand_decoder.cu:476-486)
+      for (int q = 0; q < cd.mw; ++q) {
+        uint32_t word = A.eb[q];
+        while (word) {
+          const int c = q * 32 + __ffs(word) - 1;
+          word &= word - 1u;
+          if (lane < cd.nw) s_lane ^= __ldg(cd.cols + (size_t)c * cd.nwp + lane);
+        }
+      }
+    } else {
+      for (int q = 0; q < cd.nw; ++q) {
+        const int r = q * 32 + lane;
+        const int v = r < cd.R ? rec[r] : 0;
+        const uint32_t bits = __ballot_sync(kFull, v != 0);
+        if (lane == q) s_lane = bits;
+      }
+      if (cd.family == kDem) {
+        const int *lg = b.in_log ? b.in_log + (size_t)shot * cd.n_logicos : rec + cd.R;
+        for (int q = 0; q < cd.nlw; ++q) {
+          const int j = q * 32 + lane;
+          const int v = j < cd.n_logicos ? lg[j] : 0;
+          const uint32_t bits = __ballot_sync(kFull, v != 0);
+          if (lane == 0) A.eb[q] = bits;
+        }
+      }
+    }
+    if (lane < 32) A.sw[lane] = (lane < cd.nw) ? s_lane : 0u;
+    int ws = __popc(s_lane);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) ws += __shfl_xor_sync(kFull, ws, o);
+    __syncwarp();
+
+    if (ws == 0) {  // grand_decoder.cu:1223-1241: nothing to search
+      if (lane == 0) {
+        GrandDecoderResult r = {};
+        r.original_weight = original_weight;
+        r.hibrido = -2;
+        b.results[shot] = r;
+        if (b.ml_cost) b.ml_cost[shot] = 0.0f;
+      }
+      if (b.dec_err)
+        for (int c = lane; c < cd.m; c += 32) b.dec_err[(size_t)shot * cd.m + c] = 0;
+      if (b.dec_log && cd.family == kDem)
+        for (int j = lane; j < cd.n_logicos; j += 32) b.dec_log[(size_t)shot * cd.n_logicos + j] = 0;
+      if (b.deferred) b.deferred[shot] = 0;
+      __syncwarp();
+      continue;
+    }
+
+    // ---- flagged-check counts and threshold masks ---------------------------
+    const int L = cd.max_soma < kMaxIters ? cd.max_soma : kMaxIters;
+    int tam_raw[3] = {0, 0, 0};
+    for (int q = 0; q < cd.mw; ++q) {
+      const int c = q * 32 + lane;
+      int sum = 0;
+      if (c < cd.m) {
+        const uint32_t *col = cd.cols + (size_t)c * cd.nwp;
+        for (int k = 0; k < cd.nw; ++k) sum += __popc(__ldg(col + k) & A.sw[k]);
+        if (!cd.regular) {
+          const int cw = __ldg(cd.colw + c);
+          sum = cw == 0 ? 0 : sum + (cd.max_soma - cw);
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < kMaxIters; ++i) {
+        const uint32_t bits = __ballot_sync(kFull, c < cd.m && i < L && sum >= cd.max_soma - i);
+        if (lane == 0) A.am[i][q] = bits;
+        tam_raw[i] += __popc(bits);
+      }
+    }
+    if (lane == 0) {
+      plan_shot(cd, b.ncr, tam_raw, L, b.tile_k, J);
+      J.shot = shot;
+      J.code = ci;
+      J.original_weight = original_weight;
+      J.best = kNone;
+      J.chunks_done = 0;
+    }
+    __syncwarp();
+
+    // ---- light or heavy ------------------------------------------------------
+    unsigned long long total = 0;
+    bool light = true;
+    for (int ii = 0; ii < J.n_it; ++ii) {
+      total += J.it[ii].total;
+      if (J.it[ii].tam > kLightTam || J.it[ii].tam * cd.nwp > kLightWords) light = false;
+    }
+    if (total > (1ull << b.light_max_log2)) light = false;
+    const bool ml = cd.variant == kMl;
+    const uint32_t *ebits = A.eb;
+
+    if (light) {
+      Winner wn;
+      wn.found = 0;
+      wn.ii = wn.seg = 0;
+      wn.rank = wn.count = 0;
+      wn.cost = 0.0f;
+      for (int ii = 0; ii < J.n_it && !wn.found; ++ii) {
+        IterInfo &I = J.it[ii];
+        stage_iteration(cd, A.am[I.src], I.tam, A.pos, A.tmp, A.cols, A.llr);
+        if (lane == 0) {
+          I.pos = A.pos;
+          I.cols = A.cols;
+          I.llr = A.llr;
+          if (ml) {
+            float pf = 0.0f;
+            I.prefix[0] = 0.0f;
+            for (int w = 1; w <= kMaxW; ++w) {
+              if (w <= I.tam) pf = __fadd_rn(pf, A.llr[w - 1]);
+              I.prefix[w] = pf;
+            }
+          }
+        }
+        __syncwarp();
+        if (!ml) {
+          for (int s = I.seg_lo; s < I.seg_hi && !wn.found; ++s) {
+            const Seg &S = J.seg[s];
+            if (S.dup) continue;
+            SegView sv{A.cols, A.llr, I.tam, S.w, S.K, cd.nwp, cd.nw, S.nprefix, S.base};
+            LaneBest lb;
+            lb.reset();
+            for (unsigned long long tile = 0; tile < S.ntiles; ++tile)
+              eval_dispatch<false>(cd.nw, sv, b.ncr, A.sw, tile, lb);
+            const unsigned long long g = warp_min_u64(lb.g);
+            if (g != kNone) wn = winner_from_index(J, g, cd.variant == kProb);
+          }
+        } else {
+          // upstream search_cpu_ml (grand_decoder.cu:620-656), one weight at a time
+          uint32_t bo = 0xffffffffu;
+          unsigned long long br = kNone, proc = 0;
+          int bseg = -1;
+          for (int s = I.seg_lo; s < I.seg_hi; ++s) {
+            const Seg &S = J.seg[s];
+            if (bseg >= 0 && I.prefix[S.w] >= key_cost(bo)) break;
+            proc += S.count;
+            SegView sv{A.cols, A.llr, I.tam, S.w, S.K, cd.nwp, cd.nw, S.nprefix, S.base};
+            LaneBest lb;
+            lb.reset();
+            for (unsigned long long tile = 0; tile < S.ntiles; ++tile)
+              eval_dispatch<true>(cd.nw, sv, b.ncr, A.sw, tile, lb);
+            uint32_t o = lb.o;
+            unsigned long long r = lb.r;
+            warp_min_key(o, r);
+            if (o != 0xffffffffu && (bseg < 0 || o < bo)) {
+              bo = o;
+              br = r;
+              bseg = s;
+            }
+          }
+          if (bseg >= 0) {
+            wn.found = 1;
+            wn.ii = ii;
+            wn.seg = bseg;
+            wn.rank = br;
+            wn.count = (I.branch == kBranchCpu) ? proc : I.total;
+            wn.cost = key_cost(bo);
+          }
+        }
+      }
+      finish_shot(b, cd, J, shot, wn, ebits, A.delta);
+      if (b.deferred && lane == 0) b.deferred[shot] = 0;
+      __syncwarp();
+      continue;
+    }
+
+    // ---- heavy: publish a Job ------------------------------------------------
+    unsigned long long words = 0;
+    for (int ii = 0; ii < J.n_it; ++ii) {
+      const unsigned long long tm = (unsigned long long)J.it[ii].tam;
+      words += (tm * cd.nwp + 3ull) & ~3ull;       // columns
+      words += ((ml ? 2ull : 1ull) * tm + 3ull) & ~3ull;  // positions (+ sort buffer)
+      if (ml) words += (tm + 3ull) & ~3ull;        // LLRs
+    }
+    words += 128;  // supplied bits
+    unsigned long long off = 0, jslot = 0, cbase = 0, nch = 0;
+    int ok = 1;
+    if (lane == 0) {
+      for (int s = 0; s < J.nseg; ++s) {
+        Seg &S = J.seg[s];
+        S.nchunks = S.dup ? 0ull : (S.ntiles + kTilesPerChunk - 1) / kTilesPerChunk;
+        S.chunk_lo = nch;
+        nch += S.nchunks;
+      }
+      off = atomicAdd(&b.counters[2], words);
+      if (off + words > b.scratch_words) ok = 0;
+      if (ok) {
+        const unsigned long long old = atomicAdd(&b.counters[0], (1ull << 40) | nch);
+        jslot = old >> 40;
+        cbase = old & ((1ull << 40) - 1ull);
+        if (jslot >= (unsigned long long)b.max_jobs) ok = 0;
+      }
+      if (!ok) atomicOr(b.status, ok ? 0u : kStatusJobOverflow);
+    }
+    ok = __shfl_sync(kFull, ok, 0);
+    if (!ok) {
+      if (lane == 0 && b.deferred) b.deferred[shot] = 1;
+      __syncwarp();
+      continue;
+    }
+    off = __shfl_sync(kFull, off, 0);
+    jslot = __shfl_sync(kFull, jslot, 0);
+    cbase = __shfl_sync(kFull, cbase, 0);
+    nch = __shfl_sync(kFull, nch, 0);
+    uint32_t *sp = b.scratch + off;
+    for (int ii = 0; ii < J.n_it; ++ii) {
+      IterInfo &I = J.it[ii];
+      const unsigned long long tm = (unsigned long long)I.tam;
+      uint32_t *cols = sp;
+      sp += (tm * cd.nwp + 3ull) & ~3ull;
+      int *pos = reinterpret_cast<int *>(sp);
+      int *tmp = pos + tm;
+      sp += ((ml ? 2ull : 1ull) * tm + 3ull) & ~3ull;
+      float *llr = nullptr;
+      if (ml) {
+        llr = reinterpret_cast<float *>(sp);
+        sp += (tm + 3ull) & ~3ull;
+      }
+      stage_iteration(cd, A.am[I.src], I.tam, pos, tmp, cols, llr);
+      if (lane == 0) {
+        I.pos = pos;
+        I.cols = cols;
+        I.llr = llr;
+        if (ml) {
+          float pf = 0.0f;
+          I.prefix[0] = 0.0f;
+          for (int w = 1; w <= kMaxW; ++w) {
+            if (w <= I.tam) pf = __fadd_rn(pf, llr[w - 1]);
+            I.prefix[w] = pf;
+          }
+        }
+      }
+      __syncwarp();
+    }
+    for (int q = lane; q < 128; q += 32) sp[q] = A.eb[q];
+    for (int q = lane; q < kMaxRows / 32; q += 32) J.sw[q] = A.sw[q];
+    if (lane == 0) {
+      J.ebits = sp;
+      J.chunk_base = cbase;
+      J.nchunks = nch;
+      for (int i = 0; i < kMaxIters; ++i)
+        for (int w = 0; w <= kMaxW; ++w) J.mlkey[i][w][0] = J.mlkey[i][w][1] = kNone;
+    }
+    __syncwarp();
+    {
+      const uint32_t *src = reinterpret_cast<const uint32_t *>(&J);
+      uint32_t *dst = reinterpret_cast<uint32_t *>(b.jobs + jslot);
+      for (int i = lane; i < (int)(sizeof(Job) / 4); i += 32) dst[i] = src[i];
+    }
+    if (lane == 0 && b.deferred) b.deferred[shot] = 0;
+    __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Kernel 2: persistent work-stealing search over the Jobs' chunks.
+// ---------------------------------------------------------------------------
+__device__ bool chunk_skip(const Job &J, const Seg &S, const IterInfo &I, bool ml) {
+  if (!ml) {
+    const unsigned long long best = *reinterpret_cast<const volatile unsigned long long *>(&J.best);
+    return S.base >= best;
+  }
+  for (int i = 0; i < S.iter; ++i)
+    for (int w = 1; w <= kMaxW; ++w)
+      if (*reinterpret_cast<const volatile unsigned long long *>(&J.mlkey[i][w][0]) != kNone)
+        return true;
+  for (int w = 1; w < S.w; ++w) {
+    const unsigned long long o =
+        *reinterpret_cast<const volatile unsigned long long *>(&J.mlkey[S.iter][w][0]);
+    if (o != kNone && I.prefix[S.w] >= key_cost((uint32_t)o)) return true;
+  }
+  return false;
+}
+
+__device__ Winner winner_ml(const Job &J) {
+  Winner wn;
+  wn.found = 0;
+  wn.ii = wn.seg = 0;
+  wn.rank = wn.count = 0;
+  wn.cost = 0.0f;
+  for (int ii = 0; ii < J.n_it; ++ii) {
+    const IterInfo &I = J.it[ii];
+    uint32_t bo = 0xffffffffu;
+    unsigned long long br = kNone, proc = 0;
+    int bseg = -1;
+    for (int s = I.seg_lo; s < I.seg_hi; ++s) {
+      const Seg &S = J.seg[s];
+      if (bseg >= 0 && I.prefix[S.w] >= key_cost(bo)) break;
+      proc += S.count;
+      const unsigned long long o = J.mlkey[ii][S.w][0];
+      if (o != kNone && (bseg < 0 || (uint32_t)o < bo)) {
+        bo = (uint32_t)o;
+        br = J.mlkey[ii][S.w][1];
+        bseg = s;
+      }
+    }
+    if (bseg >= 0) {
+      wn.found = 1;
+      wn.ii = ii;
+      wn.seg = bseg;
+      wn.rank = br;
+      wn.count = (I.branch == kBranchCpu) ? proc : I.total;
+      wn.cost = key_cost(bo);
+      return wn;
+    }
+  }
+  return wn;
+}
+
+__global__ void __launch_bounds__(kSearchThreads) search_kernel(DevBatch b) {
+  __shared__ __align__(16) uint32_t s_cols[kStageWords];
+  __shared__ uint32_t s_sw[kMaxRows / 32];
+  __shared__ uint32_t s_delta[kMaxCols / 32];
+  __shared__ unsigned long long s_chunk;
+  __shared__ int s_job, s_seg, s_skip, s_final, st_job, st_it;
+
+  const int tid = threadIdx.x;
+  const int lane = tid & 31;
+  const int warp = tid >> 5;
+  const unsigned long long packed = *reinterpret_cast<volatile unsigned long long *>(b.counters);
+  unsigned long long njobs = packed >> 40;
+  unsigned long long total = packed & ((1ull << 40) - 1ull);
+  if (njobs > (unsigned long long)b.max_jobs) {
+    njobs = b.max_jobs;
+    total = njobs ? b.jobs[njobs - 1].chunk_base + b.jobs[njobs - 1].nchunks : 0ull;
+  }
+  if (tid == 0) st_job = -1;
+
+  for (;;) {
+    if (tid == 0) {
+      const unsigned long long c = atomicAdd(&b.counters[1], 1ull);
+      s_chunk = c;
+      if (c < total) {
+        int lo = 0, hi = (int)njobs - 1;
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (b.jobs[mid].chunk_base <= c) lo = mid;
+          else hi = mid - 1;
+        }
+        s_job = lo;
+        const Job &J = b.jobs[lo];
+        const unsigned long long lc = c - J.chunk_base;
+        int sg = 0;
+        while (sg < J.nseg - 1 &&
+               !(lc >= J.seg[sg].chunk_lo && lc < J.seg[sg].chunk_lo + J.seg[sg].nchunks))
+          ++sg;
+        s_seg = sg;
+        const DevCode &cd = b.codes[J.code];
+        s_skip = chunk_skip(J, J.seg[sg], J.it[J.seg[sg].iter], cd.variant == kMl) ? 1 : 0;
+      }
+    }
+    __syncthreads();
+    if (s_chunk >= total) break;
+
+    Job &J = b.jobs[s_job];
+    const Seg &S = J.seg[s_seg];
+    const IterInfo &I = J.it[S.iter];
+    const DevCode &cd = b.codes[J.code];
+    const bool ml = cd.variant == kMl;
+    const bool staged = I.tam * cd.nwp <= kStageWords;
+
+    if (!s_skip && staged && (st_job != s_job || st_it != S.iter)) {
+      const uint4 *src = reinterpret_cast<const uint4 *>(I.cols);
+      uint4 *dst = reinterpret_cast<uint4 *>(s_cols);
+      const int n4 = (I.tam * cd.nwp + 3) / 4;
+      for (int i = tid; i < n4; i += kSearchThreads) dst[i] = src[i];
+      for (int i = tid; i < kMaxRows / 32; i += kSearchThreads) s_sw[i] = J.sw[i];
+      __syncthreads();
+      if (tid == 0) {
+        st_job = s_job;
+        st_it = S.iter;
+      }
+    } else if (!s_skip && !staged) {
+      for (int i = tid; i < kMaxRows / 32; i += kSearchThreads) s_sw[i] = J.sw[i];
+      if (tid == 0) st_job = -1;
+    }
+    __syncthreads();
+
+    if (!s_skip) {
+      const unsigned long long lc = s_chunk - J.chunk_base - S.chunk_lo;
+      const unsigned long long t0 = lc * kTilesPerChunk;
+      unsigned long long t1 = t0 + kTilesPerChunk;
+      if (t1 > S.ntiles) t1 = S.ntiles;
+      SegView sv{staged ? s_cols : I.cols, I.llr, I.tam, S.w, S.K, cd.nwp, cd.nw, S.nprefix,
+                 S.base};
+      LaneBest lb;
+      lb.reset();
+      for (unsigned long long tile = t0 + warp; tile < t1; tile += kSearchWarps) {
+        if (ml) eval_dispatch<true>(cd.nw, sv, b.ncr, s_sw, tile, lb);
+        else eval_dispatch<false>(cd.nw, sv, b.ncr, s_sw, tile, lb);
+      }
+      if (!ml) {
+        const unsigned long long g = warp_min_u64(lb.g);
+        if (lane == 0 && g != kNone) atomicMin(&J.best, g);
+      } else {
+        uint32_t o = lb.o;
+        unsigned long long r = lb.r;
+        warp_min_key(o, r);
+        if (lane == 0 && o != 0xffffffffu)
+          if (!atomic_min_key(J.mlkey[S.iter][S.w], o, r)) atomicOr(b.status, kStatusCasLimit);
+      }
+    }
+    __syncthreads();
+    if (tid == 0) {
+      __threadfence();
+      const unsigned long long d = atomicAdd(&J.chunks_done, 1ull);
+      s_final = (d + 1ull == J.nchunks) ? 1 : 0;
+    }
+    __syncthreads();
+    if (s_final && warp == 0) {
+      __threadfence();
+      Winner wn;
+      if (!ml)
+        wn = winner_from_index(J, *reinterpret_cast<volatile unsigned long long *>(&J.best),
+                               cd.variant == kProb);
+      else wn = winner_ml(J);
+      finish_shot(b, cd, J, J.shot, wn, J.ebits, s_delta);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host-callable launchers.
+// ---------------------------------------------------------------------------
+cudaError_t launch_triage(const DevBatch &b, int grid, cudaStream_t s) {
+  triage_kernel<<<grid, kTriageWarps * 32, 0, s>>>(b);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_search(const DevBatch &b, int grid, cudaStream_t s) {
+  search_kernel<<<grid, kSearchThreads, 0, s>>>(b);
+  return cudaGetLastError();
+}
+
+int triage_warps_per_block() { return kTriageWarps; }
+int search_threads_per_block() { return kSearchThreads; }
+
+cudaError_t occupancy(int *triage_blocks_per_sm, int *search_blocks_per_sm) {
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(triage_blocks_per_sm, triage_kernel,
+                                                                kTriageWarps * 32, 0);
+  if (e != cudaSuccess) return e;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(search_blocks_per_sm, search_kernel,
+                                                       kSearchThreads, 0);
+}
+
+}  // namespace grand
