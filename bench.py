@@ -1,0 +1,427 @@
+#!/usr/bin/env python
+"""GRAND decoder benchmark on GB300.
+
+Workload (one step = one batch): grand_decode_prob_cc on the bivariate-bicycle
+code [[144,12,12]] (Hz 72 x 144), X errors with per-qubit probabilities
+log-uniform in [1e-3, 1e-2], 16384 shots, max_error_weight 4, active-position
+cap 64, phase mask "300 0 1 2" (upstream: phase 0 = weights 1..5).  Seeded
+synthetic data (numpy PCG64); no dataset exists for this workload.
+
+Reported (one JSON line, rank 0):
+  value      shots/s of the persistent batched decoder, records resident in HBM,
+             graph-replayed triage + search launches, L2 flushed between steps;
+  e2e        shots/s through the upstream-compatible C ABI (grand_decode_prob_cc)
+             from host buffers, copies included;
+  roofline   the search kernel on the stress input the integer roofline is
+             defined on (random syndromes, W = 4, exhaustive enumeration), ops
+             counted as (w+1)*ceil(R/32) per candidate, against the measured
+             lop3 issue rate of this GPU;
+  cpu_baseline  the upstream CPU search algorithm (its C restatement in oracle/,
+             or the upstream library itself where it was built) on all host cores.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "shots/s & candidates/s, BB n=144 w≤4, plain vs persistent; p50/p99 latency"
+SHOTS = 16384
+W_MAX = 4
+CAP = 64
+PHASE = [(300, 0, 1, 2, 1.0, 0.0, 0.0)]
+FLUSH_BYTES = 256 << 20
+
+
+def workload(seed: int):
+    from library_s_grand_gb300 import synth
+    code = synth.BB_CODES[144]()
+    rng = np.random.default_rng(0)
+    p = np.exp(rng.uniform(np.log(1e-3), np.log(1e-2), code.m))
+    errors, _ = synth.css_shots(code.hz, SHOTS, p, seed=1 + seed)
+    return code, errors
+
+
+def workload_config():
+    return {"workload": "grand_decode_prob_cc BB[[144,12,12]] Hz 72x144, X errors p_i log-uniform "
+                        "[1e-3,1e-2], 16384 shots, W=4, cap 64, phase mask '300 0 1 2'",
+            "shots_per_step": SHOTS, "max_error_weight": W_MAX, "active_cap": CAP,
+            "mode_of_search": -1, "records": "int32 errors (144 per shot)",
+            "l2": "flushed between timed steps (256 MiB write)"}
+
+
+# ---------------------------------------------------------------------------
+# CPU side: the upstream CPU search algorithm on host cores
+# ---------------------------------------------------------------------------
+_W = {}
+
+
+def _worker_init(kind, rows, phase_path):
+    devnull = os.open(os.devnull, os.O_WRONLY)
+    os.dup2(devnull, 1)  # upstream prints one line per shot
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    code, errors = workload(0)
+    _W["lib"] = O.Reference() if kind == "reference" else O.Port()
+    _W["O"] = O
+    _W["code"] = code
+    _W["errors"] = errors[rows[0]:rows[1]]
+    _W["phase"] = phase_path
+
+
+def _worker_step(_):
+    O = _W["O"]
+    cfg = O.make_config(W_MAX, mode=-1, cap=CAP)
+    t0 = time.perf_counter()
+    r = _W["lib"].css(O.PROB, _W["code"].hx, _W["code"].hz, _W["errors"], None, cfg, "x", _W["phase"])
+    res = r[1]
+    return len(res), int(res["total_tested_combinations"].sum()), time.perf_counter() - t0
+
+
+class CpuPool:
+    """One process per host core, each owning a fixed slice of the batch."""
+
+    def __init__(self, phase_path, cores=None):
+        import multiprocessing as mp
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        O.build()
+        self.kind = "reference" if O.Reference.available() else "port"
+        self.cores = cores or os.cpu_count() or 1
+        ctx = mp.get_context("spawn")
+        bounds = np.linspace(0, SHOTS, self.cores + 1).astype(int)
+        self.pools = [ctx.Pool(1, initializer=_worker_init,
+                               initargs=(self.kind, (int(bounds[i]), int(bounds[i + 1])), phase_path))
+                      for i in range(self.cores)]
+
+    def step(self):
+        t0 = time.perf_counter()
+        futs = [p.apply_async(_worker_step, (0,)) for p in self.pools]
+        out = [f.get() for f in futs]
+        return time.perf_counter() - t0, sum(o[0] for o in out), sum(o[1] for o in out)
+
+    def close(self):
+        for p in self.pools:
+            p.terminate()
+
+
+def cpu_baseline(phase_path, seconds=12.0):
+    pool = CpuPool(phase_path)
+    try:
+        pool.step()  # warm-up (imports, library load)
+        t_tot, shots, cands, steps = 0.0, 0, 0, 0
+        while t_tot < seconds and steps < 10000:
+            dt, s, c = pool.step()
+            t_tot += dt
+            shots += s
+            cands += c
+            steps += 1
+    finally:
+        pool.close()
+    return {"value": shots / t_tot, "unit": "shots/s", "cores": pool.cores, "kind": pool.kind,
+            "candidates_per_s": cands / t_tot,
+            "sample": f"{steps} passes over the 16384-shot batch split across {pool.cores} "
+                      f"processes ({t_tot:.1f} s wall), upstream CPU search algorithm, mode -1"}
+
+
+# ---------------------------------------------------------------------------
+# Clocks during the timed region
+# ---------------------------------------------------------------------------
+class Clocks:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.path = tempfile.mktemp(suffix=".csv")
+        self.device = device
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": float(max(mx)) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def stress_ops(code_h, syndromes, W):
+    """Exhaustive search work of random-syndrome shots: (candidates, ops) with
+    ops = (w+1)*ceil(R/32) per weight-w candidate, iteration sets as upstream."""
+    R = code_h.shape[0]
+    words = math.ceil(R / 32)
+    colw = code_h.sum(axis=0)
+    max_soma = int(colw.max())
+    sums = syndromes.astype(np.int64) @ code_h.astype(np.int64)
+    cands = ops = 0
+    for s in sums:
+        for it in range(min(max_soma, 3)):
+            tam = int((s >= max_soma - it).sum())
+            for w in range(1, min(W, 6) + 1):
+                c = math.comb(tam, w)
+                cands += c
+                ops += c * (w + 1) * words
+    return cands, ops
+
+
+def run_ours(args):
+    import torch
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from library_s_grand_gb300 import build as B
+    from library_s_grand_gb300 import capi, synth
+    from library_s_grand_gb300.engine import Engine
+
+    B.build()
+    lib = capi.load_library()
+    eng = Engine(lib)
+    tmp = tempfile.mkdtemp()
+    phase = synth.write_phase_file(os.path.join(tmp, "phase.txt"), PHASE)
+    code, errors = workload(rank)
+    cfg = capi.GrandDecoderConfig(W_MAX, 256, 0, CAP, 10, -1)
+    eng.add_css(code.hx, code.hz, "x", True, cfg, phase)
+
+    dev = torch.device("cuda", local)
+    d_rec = torch.from_numpy(np.ascontiguousarray(errors.ravel())).to(dev)
+    d_res = torch.empty(SHOTS * 72, dtype=torch.uint8, device=dev)
+    flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    sp = stream.cuda_stream
+
+    def step():
+        rc = eng.decode_device(SHOTS, d_rec.data_ptr(), d_res.data_ptr(), sp, use_graph=True)
+        if rc != 0:
+            raise RuntimeError(f"device decode failed ({rc})")
+
+    for _ in range(args.warmup):
+        flush.fill_(1)
+        step()
+    if eng.sync_status(sp) != 0:
+        raise RuntimeError("device decode status error")
+    # one checked pass: device results equal the C ABI's
+    res_dev = np.frombuffer(d_res.cpu().numpy().tobytes(), dtype=capi.RESULT_DTYPE)
+    rc, res_c, _ = capi.decode_css_ex(lib, "prob", code.hx, code.hz, errors, None, cfg, "x", phase)
+    assert rc == 0
+    for f in ("found", "found_weight", "tam", "total_tested_combinations", "iteration", "degenerate"):
+        assert np.array_equal(res_dev[f], res_c[f]), f
+    cands_step = int(res_c["total_tested_combinations"].sum())
+
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    clocks = Clocks(local)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    time.sleep(0.3)
+    for i in range(args.steps):
+        flush.fill_(i & 255)
+        ev[i][0].record(stream)
+        step()
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    time.sleep(0.2)
+    clk = clocks.stop()
+    if dist:
+        dist.barrier()
+    if eng.sync_status(sp) != 0:
+        raise RuntimeError("device decode status error")
+    per = np.array([a.elapsed_time(b) for a, b in ev])
+    total_ms = float(per.sum())
+    if dist:
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * SHOTS * args.steps / (total_ms * 1e-3)
+
+    # kernel split (non-graph launch with events)
+    eng.decode_device(SHOTS, d_rec.data_ptr(), d_res.data_ptr(), sp, use_graph=False)
+    eng.sync_status(sp)
+    tri_ms, sea_ms = eng.kernel_times(sp)
+
+    out = None
+    if rank == 0:
+        # e2e through the upstream-compatible C ABI, host buffers in and out
+        e_flat = np.ascontiguousarray(errors, dtype=np.int32)
+        hx = np.ascontiguousarray(code.hx, dtype=np.int32)
+        hz = np.ascontiguousarray(code.hz, dtype=np.int32)
+        k_e2e = max(3, min(args.steps, 200))
+        for _ in range(3):
+            rc, _ = capi.run_grand_prob_shots_cc(lib, hx, hz, e_flat, None, cfg, phase, b"x")
+        torch.cuda.synchronize()
+        lat = []
+        t0 = time.perf_counter()
+        for _ in range(k_e2e):
+            a = time.perf_counter()
+            rc, _ = capi.run_grand_prob_shots_cc(lib, hx, hz, e_flat, None, cfg, phase, b"x")
+            lat.append(time.perf_counter() - a)
+            assert rc == 0
+        e2e_s = time.perf_counter() - t0
+        e2e = {"value": SHOTS * k_e2e / e2e_s, "unit": "shots/s",
+               "h2d_bytes_per_step": SHOTS * code.m * 4, "d2h_bytes_per_step": SHOTS * 72,
+               "steps": k_e2e, "p50_ms": float(np.percentile(lat, 50) * 1e3),
+               "p99_ms": float(np.percentile(lat, 99) * 1e3)}
+
+        # plain one-launch-per-call path (per shot), on a 1024-shot slice
+        n_plain = 1024
+        rc, _ = eng.decode_plain(errors[:64].ravel(), num_shots=64)
+        t0 = time.perf_counter()
+        rc, res_plain = eng.decode_plain(errors[:n_plain].ravel(), num_shots=n_plain)
+        plain_s = time.perf_counter() - t0
+        assert rc == 0
+        assert np.array_equal(res_plain["total_tested_combinations"],
+                              res_c["total_tested_combinations"][:n_plain])
+
+        roof = stress_roofline(torch, lib, dev, sp)
+        cpu = cpu_baseline(phase, seconds=args.cpu_seconds) if args.cpu_seconds > 0 else None
+
+        out = {
+            "metric": METRIC, "value": value, "unit": "shots/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+            "data": "synthetic (seeded numpy PCG64)", "config": workload_config(),
+            "candidates_per_s": world * cands_step * args.steps / (total_ms * 1e-3),
+            "candidates_per_step": cands_step,
+            "latency_ms": {"p50": float(np.percentile(per, 50)), "p99": float(np.percentile(per, 99)),
+                           "what": "per 16384-shot batch, device-resident, graph replay"},
+            "plain_shots_per_s": n_plain / plain_s,
+            "plain_what": "one call per shot: H2D record, triage+search launches, sync, D2H",
+            "persistent_vs_plain": value / world / (n_plain / plain_s),
+            "kernel_ms": {"triage": tri_ms, "search": sea_ms},
+            "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
+            "gpu_launches": 2 * args.steps,
+        }
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    return out
+
+
+def stress_roofline(torch, lib, dev, sp):
+    """Search kernel on exhaustive random-syndrome shots of [[144,12,12]], W=4."""
+    from library_s_grand_gb300 import capi, synth
+    from library_s_grand_gb300.engine import Engine
+    code = synth.BB_CODES[144]()
+    n = 192
+    syn = (np.random.default_rng(1).random((n, code.n)) < 0.5).astype(np.int32)
+    cands, ops = stress_ops(code.hz, syn, 4)
+    eng = Engine(lib)
+    eng.add_css(code.hx, code.hz, "x", False, capi.GrandDecoderConfig(4, 256, 0, 300, 10, -1))
+    d_rec = torch.from_numpy(syn.ravel()).to(dev)
+    d_res = torch.empty(n * 72, dtype=torch.uint8, device=dev)
+    times = []
+    for rep in range(4):
+        eng.decode_device(n, d_rec.data_ptr(), d_res.data_ptr(), sp, use_graph=False)
+        if eng.sync_status(sp) != 0:
+            raise RuntimeError("stress decode failed")
+        times.append(eng.kernel_times(sp)[1])
+    res = np.frombuffer(d_res.cpu().numpy().tobytes(), dtype=capi.RESULT_DTYPE)
+    assert int(res["found"].sum()) == 0
+    assert int(res["total_tested_combinations"].sum()) == cands, "count mismatch"
+    search_ms = float(np.median(times[1:]))
+    peak = eng.int_peak()
+    achieved = ops / (search_ms * 1e-3)
+    return {"bound": "int_alu", "achieved": achieved / 1e9, "peak": peak / 1e9, "unit": "Gop/s",
+            "frac": achieved / peak, "traffic": None, "kernel": "search_kernel",
+            "workload": f"{n} random-syndrome shots of BB[[144,12,12]], W=4, exhaustive "
+                        f"({cands} candidates, 3 threshold iterations)",
+            "ops_per_candidate": "(w+1)*ceil(72/32)", "search_ms": search_ms,
+            "candidates_per_s": cands / (search_ms * 1e-3),
+            "peak_source": "lop3.b32 issue rate measured on this GPU (grand_measure_int_peak)"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return None
+    from library_s_grand_gb300 import synth
+    tmp = tempfile.mkdtemp()
+    phase = synth.write_phase_file(os.path.join(tmp, "phase.txt"), PHASE)
+    pool = CpuPool(phase)
+    try:
+        for _ in range(args.warmup):
+            pool.step()
+        t_tot, cands = 0.0, 0
+        for _ in range(args.steps):
+            dt, s, c = pool.step()
+            t_tot += dt
+            cands += c
+    finally:
+        pool.close()
+    value = SHOTS * args.steps / t_tot
+    return {"metric": METRIC, "value": value, "unit": "shots/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_tot * 1e3 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic (seeded numpy PCG64)", "config": workload_config(),
+            "impl": "reference", "candidates_per_s": cands / t_tot,
+            "cpu_baseline": {"value": value, "unit": "shots/s", "cores": pool.cores,
+                             "kind": pool.kind,
+                             "sample": f"{args.steps} timed passes over the 16384-shot batch split "
+                                       f"across {pool.cores} processes, mode -1"},
+            "e2e": {"value": value, "unit": "shots/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    out = run_reference(args) if args.impl == "reference" else run_ours(args)
+    if out is not None:
+        print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,101 @@
+/*
+ * grand_engine.h -- batched, mixed-code decoding with device-resident codes.
+ *
+ * No upstream counterpart: upstream decodes one code per call with a serial
+ * host loop over shots (grand_decoder.cu:885, 1199, 1466, 1762, 2073).  An
+ * engine keeps any number of registered codes resident on the GPU and decodes
+ * batches whose shots may use different codes, in one triage launch plus one
+ * persistent work-stealing search launch, optionally replayed from a captured
+ * CUDA graph.  Results are identical to the five grand_decode_* calls on the
+ * same shots.
+ *
+ * Shot records are int32 0/1 rows: the syndrome (n entries) or the error (m
+ * entries) for CSS codes, as chosen at registration; the detectors followed by
+ * the true logical flips (n + n_logicos entries) for DEM codes.
+ */
+#ifndef GRAND_ENGINE_H
+#define GRAND_ENGINE_H
+
+#include "grand_decoder.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct GrandEngine GrandEngine;
+
+/* Variant selector for grand_engine_add_dem. */
+#define GRAND_VARIANT_UNIFORM 0
+#define GRAND_VARIANT_PROB    1
+#define GRAND_VARIANT_ML      2
+
+/* Create an engine on the current CUDA device. */
+int grand_engine_create(GrandEngine **engine);
+void grand_engine_destroy(GrandEngine *engine);
+
+/* Register a CSS code.  probability_file == NULL selects the uniform search
+ * (grand_decode_cc), otherwise the phase-ordered one (grand_decode_prob_cc).
+ * records_are_errors != 0: records hold errors (m entries), else syndromes. */
+int grand_engine_add_css(GrandEngine *engine, const int *Hx, const int *Hz, int n, int m,
+                         char type_of_error, int records_are_errors,
+                         const GrandDecoderConfig *config, const char *probability_file,
+                         int *code_id);
+
+/* Register a DEM code (grand_decode_cln / _prob_cln / _ML_cln semantics);
+ * file is the phase-mask file (PROB) or the LLR file (ML), else NULL. */
+int grand_engine_add_dem(GrandEngine *engine, const int *H_dem, const int *L_dem, int n, int m,
+                         int n_logicos, const GrandDecoderConfig *config, int variant,
+                         const char *file, int *code_id);
+
+/* int32 entries per shot record of a registered code (or < 0). */
+int grand_engine_record_len(GrandEngine *engine, int code_id);
+
+/* Decode num_shots records, concatenated in shot order, from host memory.
+ * shot_code may be NULL when every shot uses code 0.  Synchronous. */
+int grand_engine_decode(GrandEngine *engine, int num_shots, const int *shot_code,
+                        const int *records, GrandDecoderResult *results,
+                        const GrandDecodeOutputs *out);
+
+/* Device-resident decode, asynchronous on `stream` (a cudaStream_t; NULL is
+ * the legacy default stream).  All pointers are device pointers; d_offsets
+ * (int64 record offsets) and d_shot_code may be NULL when every shot uses code
+ * 0.  With use_graph != 0 the launch sequence is captured into a CUDA graph on
+ * first use for this argument set and replayed afterwards.  Call
+ * grand_engine_sync_status() to wait and read the completion status. */
+int grand_engine_decode_device(GrandEngine *engine, int num_shots, const int *d_shot_code,
+                               const long long *d_offsets, const int *d_records,
+                               GrandDecoderResult *d_results, void *stream, int use_graph);
+
+/* Wait for `stream` and return 0, or a GRAND_ERR_* code when the last device
+ * decode on it hit a kernel limit (job table / scratch overflow, active set
+ * beyond GRAND_MAX_TAM). */
+int grand_engine_sync_status(GrandEngine *engine, void *stream);
+
+/* The reference-style one-launch-per-call path: every shot is its own call
+ * (host-to-device copy of its record, its triage and search launches, a
+ * synchronous read-back of its result), as upstream's GPU mode does per shot.
+ * Kept for comparison with the batched path. */
+int grand_engine_decode_plain(GrandEngine *engine, int num_shots, const int *shot_code,
+                              const int *records, GrandDecoderResult *results);
+
+/* Tuning knobs (also set by the GRAND_* environment variables):
+ * light_log2: largest per-shot search (2^x candidates) finished inside the
+ * triage warp; tile_k: prefixes per lane per search tile; search_ctas_per_sm:
+ * resident CTAs of the persistent search kernel (0 = occupancy maximum). */
+int grand_engine_set_tuning(GrandEngine *engine, int light_log2, int tile_k,
+                            int search_ctas_per_sm);
+
+/* Device times of the triage and search kernels of the last non-graph device
+ * decode on `stream` (valid after grand_engine_sync_status). */
+int grand_engine_kernel_times(GrandEngine *engine, void *stream, float *triage_ms,
+                              float *search_ms);
+
+/* Diagnostic: sustained 32-bit logic-op (lop3) issue rate of the current device
+ * in ops/s, the ceiling of the search kernel's integer roofline; < 0 on error. */
+double grand_measure_int_peak(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GRAND_ENGINE_H */

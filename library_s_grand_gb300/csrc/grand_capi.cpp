@@ -15,8 +15,6 @@
 namespace grand {
 const char *last_error();
 
-namespace {
-
 struct Masks {
   int n = 0;
   int tam_upper[kMaxMasks];
@@ -76,6 +74,28 @@ int num_phases_for(int W) {  // grand_decoder.cu:852-868
   if (W > 0 && W < 6) return 1;
   return 0;
 }
+
+bool read_llr_file(const char *path, std::vector<float> &llr, int m) { return read_llr(path, llr, m); }
+
+// Phase masks for a registered code: the upstream checks, in upstream order.
+int read_masks_into(const char *path, CallParams *p, int W) {
+  Masks mk = read_masks(path);
+  p->num_phases = num_phases_for(W);
+  if (p->num_phases == 0) {
+    fprintf(stderr, "Invalid max_error_weight: %d. Must be 6 or 7.\n", W);
+    return GRAND_ERR_INVALID;
+  }
+  if (mk.n == 0) {
+    fprintf(stderr, "No phase order masks read from: %s\n", path ? path : "(null)");
+    return GRAND_ERR_INVALID;
+  }
+  p->n_masks = mk.n;
+  memcpy(p->mask_tam_upper, mk.tam_upper, sizeof(mk.tam_upper));
+  memcpy(p->mask_order, mk.order, sizeof(mk.order));
+  return 0;
+}
+
+namespace {
 
 bool verbose() {
   static int v = [] {

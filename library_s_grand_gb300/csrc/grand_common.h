@@ -73,9 +73,9 @@ struct Seg {
   unsigned long long base;   // first global candidate index of this block within the shot
   unsigned long long count;  // C(tam, w)
   unsigned long long nprefix;// number of (w-1)-prefixes, C(tam-1, w-1)
-  unsigned long long ntiles; // tiles of kLanes x K prefixes
-  unsigned long long chunk_lo; // first chunk of this block within the job
-  unsigned long long nchunks;
+  unsigned long long ntiles; // tiles of 32 lanes x K prefixes
+  unsigned long long tile_lo;// first tile of this block within the job (search kernel)
+  unsigned long long njt;    // tiles the search kernel runs for this block (0: none)
   int K;                     // prefixes per lane in a tile
 };
 
@@ -95,17 +95,18 @@ struct IterInfo {
 };
 
 // A shot whose search space is too large for one warp: searched by every
-// block of the persistent search kernel, chunk by chunk.  16-byte aligned: the
+// warp of the persistent search kernel, tile by tile.  16-byte aligned: the
 // ML minima are updated with 128-bit compare-and-swap.
 struct alignas(16) Job {
   int shot, code;
   int n_it;
   int nseg;
-  int final_iteration, final_tam, hib_before; // outcome fields if nothing is found
-  unsigned long long chunk_base;  // first global chunk
-  unsigned long long nchunks;
+  int final_iteration, final_tam; // outcome fields if nothing is found
+  int it_lo;                      // first iteration searched by the search kernel
+  unsigned long long tile_base;   // first global tile
+  unsigned long long ntiles;
   unsigned long long best;        // lowest matching global index (atomicMin)
-  unsigned long long chunks_done;
+  unsigned long long tiles_done;
   int original_weight;
   int failed;                     // an active set exceeded the kernel limits
   uint32_t *ebits;                // mw words: supplied error (CSS) / truth logicals (DEM)
@@ -134,7 +135,7 @@ struct DevBatch {
   const unsigned long long *ncr; // (kMaxTam + 1) x (kMaxW + 1)
   Job *jobs;
   int max_jobs;
-  unsigned long long *counters;  // [0] packed job/chunk append, [1] next chunk, [2] scratch top
+  unsigned long long *counters;  // [0] packed job/tile append, [1] next tile, [2] scratch top
   uint32_t *scratch;
   unsigned long long scratch_words;
   unsigned *status;

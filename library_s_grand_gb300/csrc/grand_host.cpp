@@ -307,7 +307,7 @@ DevCode make_devcode(const CodeTables &t, const CallParams &p) {
   d.n_logicos = t.n_logicos;
   d.nlw = t.nlw;
   d.rank = t.rank;
-  d.rec_len = p.input_kind == kInErrors ? t.m : t.R;
+  d.rec_len = p.rec_len ? p.rec_len : (p.input_kind == kInErrors ? t.m : t.R);
   d.cols = t.cols;
   d.colw = t.colw;
   d.rows = nullptr;
@@ -318,11 +318,26 @@ DevCode make_devcode(const CodeTables &t, const CallParams &p) {
   return d;
 }
 
-int run_batch(Context *ctx, Workspace *ws, const BatchRequest &req, BatchTiming *timing) {
+cudaError_t launch_pipeline(const Context *ctx, const DevBatch &b, const Tuning &tn,
+                            cudaStream_t s, cudaEvent_t mid) {
+  cudaError_t e = cudaMemsetAsync(b.counters, 0, 256, s);
+  if (e != cudaSuccess) return e;
+  const int tgrid_max = ctx->sm_count * std::max(ctx->triage_bps, 1);
+  const int tgrid = std::max(1, std::min(tgrid_max, (b.num_shots + 3) / 4));
+  e = launch_triage(b, tgrid, s);
+  if (e != cudaSuccess) return e;
+  if (mid) cudaEventRecord(mid, s);
+  const int per_sm = tn.search_grid_mult ? std::min(tn.search_grid_mult, std::max(ctx->search_bps, 1))
+                                         : std::max(ctx->search_bps, 1);
+  return launch_search(b, ctx->sm_count * per_sm, s);
+}
+
+int run_batch(Context *ctx, Workspace *ws, const BatchRequest &req, BatchTiming *timing,
+              const Tuning *tnp) {
   const int N = req.num_shots;
   if (N <= 0) return 0;
   cudaStream_t s = ws->stream;
-  const Tuning &tn = tuning();
+  const Tuning &tn = tnp ? *tnp : tuning();
   const int ncodes = (int)req.codes.size();
 
   CK(ensure(&ws->d_codes, &ws->cap_codes, sizeof(DevCode) * ncodes));
@@ -378,8 +393,6 @@ int run_batch(Context *ctx, Workspace *ws, const BatchRequest &req, BatchTiming 
   b.light_max_log2 = tn.light_max_log2;
   b.tile_k = tn.tile_k;
 
-  const int tgrid_max = ctx->sm_count * std::max(ctx->triage_bps, 1);
-  const int sgrid = ctx->sm_count * std::max(1, tn.search_grid_mult ? tn.search_grid_mult : ctx->search_bps);
   std::vector<int> map;
   int todo = N;
   float tri_ms = 0, sea_ms = 0;
@@ -388,13 +401,8 @@ int run_batch(Context *ctx, Workspace *ws, const BatchRequest &req, BatchTiming 
   for (;;) {
     b.num_shots = todo;
     b.shot_map = rounds == 0 ? nullptr : (const int *)ws->d_map;
-    CK(cudaMemsetAsync(ws->d_small, 0, 256, s));
-    const int twarps = 4;
-    const int tgrid = std::max(1, std::min(tgrid_max, (todo + twarps - 1) / twarps));
     CK(cudaEventRecord(ws->ev[2], s));
-    CK(launch_triage(b, tgrid, s));
-    CK(cudaEventRecord(ws->ev[3], s));
-    CK(launch_search(b, sgrid, s));
+    CK(launch_pipeline(ctx, b, tn, s, ws->ev[3]));
     CK(cudaEventRecord(ws->ev[4], s));
     unsigned st = 0;
     CK(cudaMemcpyAsync(&st, b.status, sizeof(unsigned), cudaMemcpyDeviceToHost, s));

@@ -46,6 +46,7 @@ struct CallParams {
   int mask_tam_upper[kMaxMasks] = {};
   int mask_order[kMaxMasks][3] = {};
   const float *d_llr = nullptr;   // device LLRs (ML)
+  int rec_len = 0;                 // int32 entries per record (0: R, or m for errors)
 };
 
 DevCode make_devcode(const CodeTables &t, const CallParams &p);
@@ -117,15 +118,20 @@ struct BatchTiming {
   int rounds = 0;
 };
 
-// Runs the batch; returns 0 or a GRAND_ERR_* code.
-int run_batch(Context *ctx, Workspace *ws, const BatchRequest &req, BatchTiming *timing);
-
 // Tunables (environment overrides, autotuner results).
 struct Tuning {
   int light_max_log2 = 12;
   int tile_k = 4;
-  int search_grid_mult = 0;  // 0: occupancy-derived
+  int search_grid_mult = 0;  // CTAs per SM of the search kernel; 0: occupancy maximum
 };
-Tuning &tuning();
+Tuning &tuning();  // process defaults (GRAND_LIGHT_LOG2, GRAND_TILE_K, GRAND_SEARCH_GRID_MULT)
+
+// Runs the batch; returns 0 or a GRAND_ERR_* code.
+int run_batch(Context *ctx, Workspace *ws, const BatchRequest &req, BatchTiming *timing,
+              const Tuning *tn = nullptr);
+
+// Enqueue one launch of the pipeline (counter reset, triage, search) on s.
+cudaError_t launch_pipeline(const Context *ctx, const DevBatch &b, const Tuning &tn,
+                            cudaStream_t s, cudaEvent_t mid = nullptr);
 
 }  // namespace grand

@@ -6,18 +6,19 @@
 //   grand_decoder.cu:67-81 / 352-374, with the irregular offset of :406-416),
 //   the active sets of the <= 3 threshold iterations (:1284-1290, :495-504),
 //   the upstream active-set cap and mode rules (:1296, :1327, :1550-1554), and
-//   the weight blocks each searched iteration enumerates.  Shots whose whole
-//   search space fits the light budget are searched and finished by the same
-//   warp; the others become Jobs for the persistent search kernel.
+//   the weight blocks each searched iteration enumerates.  The iterations are
+//   searched in upstream order by the same warp while each fits the light
+//   budget; the first larger one and those after it become a Job for the
+//   persistent search kernel.
 //
-// search_kernel (persistent, one CTA per resident slot)
-//   every CTA repeatedly takes the next chunk (a run of tiles of one weight
-//   block of one Job) from a global counter, stages the block's active columns
-//   in shared memory, lets its 8 warps evaluate the tiles, publishes the lowest
-//   matching global index (atomicMin) or the lowest {cost, rank} key (128-bit
-//   CAS), and the CTA that completes a Job's last chunk writes its result.
-//   Chunks whose candidates all rank above an already-found match are skipped.
-//   No CTA ever waits for another.
+// search_kernel (persistent, every warp an independent worker)
+//   every warp repeatedly takes the next tiles (K colex prefixes per lane of
+//   one weight block of one Job) from a global counter, stages the iteration's
+//   active columns in its own shared-memory slice, evaluates them, publishes
+//   the lowest matching global index (atomicMin) or the lowest {cost, rank}
+//   key (128-bit CAS), and the warp that completes a Job's last tile writes its
+//   result.  Tiles whose candidates all rank above an already-found match are
+//   skipped.  No warp ever waits for another: there are no block barriers.
 #include <cuda_runtime.h>
 
 #include "grand_device.cuh"
@@ -29,8 +30,8 @@ constexpr int kLightTam = 96;
 constexpr int kLightWords = kLightTam * 8;
 constexpr int kSearchThreads = 256;
 constexpr int kSearchWarps = kSearchThreads / 32;
-constexpr int kStageWords = 8192;
-constexpr int kTilesPerChunk = kSearchWarps;
+constexpr int kWarpStage = 1280;  // staged active-column words per search warp
+constexpr int kTilesPerFetch = 2;
 
 struct alignas(16) WarpArea {
   uint32_t cols[kLightWords];
@@ -330,6 +331,72 @@ __device__ __forceinline__ void eval_dispatch(int nw, const SegView &sv,
 // ---------------------------------------------------------------------------
 // Kernel 1: triage + light search.
 // ---------------------------------------------------------------------------
+__device__ void light_search(const DevBatch &b, const DevCode &cd, Job &J, WarpArea &A, int ii,
+                             Winner &wn) {
+  const int lane = threadIdx.x & 31;
+  const bool ml = cd.variant == kMl;
+  IterInfo &I = J.it[ii];
+  stage_iteration(cd, A.am[I.src], I.tam, A.pos, A.tmp, A.cols, A.llr);
+  if (lane == 0) {
+    I.pos = A.pos;
+    I.cols = A.cols;
+    I.llr = A.llr;
+    if (ml) {
+      float pf = 0.0f;
+      I.prefix[0] = 0.0f;
+      for (int w = 1; w <= kMaxW; ++w) {
+        if (w <= I.tam) pf = __fadd_rn(pf, A.llr[w - 1]);
+        I.prefix[w] = pf;
+      }
+    }
+  }
+  __syncwarp();
+  if (!ml) {
+    for (int s = I.seg_lo; s < I.seg_hi && !wn.found; ++s) {
+      const Seg &S = J.seg[s];
+      if (S.dup) continue;
+      SegView sv{A.cols, A.llr, I.tam, S.w, S.K, cd.nwp, cd.nw, S.nprefix, S.base};
+      LaneBest lb;
+      lb.reset();
+      for (unsigned long long tile = 0; tile < S.ntiles; ++tile)
+        eval_dispatch<false>(cd.nw, sv, b.ncr, A.sw, tile, lb);
+      const unsigned long long g = warp_min_u64(lb.g);
+      if (g != kNone) wn = winner_from_index(J, g, cd.variant == kProb);
+    }
+    return;
+  }
+  // upstream search_cpu_ml (grand_decoder.cu:620-656), one weight at a time
+  uint32_t bo = 0xffffffffu;
+  unsigned long long br = kNone, proc = 0;
+  int bseg = -1;
+  for (int s = I.seg_lo; s < I.seg_hi; ++s) {
+    const Seg &S = J.seg[s];
+    if (bseg >= 0 && I.prefix[S.w] >= key_cost(bo)) break;
+    proc += S.count;
+    SegView sv{A.cols, A.llr, I.tam, S.w, S.K, cd.nwp, cd.nw, S.nprefix, S.base};
+    LaneBest lb;
+    lb.reset();
+    for (unsigned long long tile = 0; tile < S.ntiles; ++tile)
+      eval_dispatch<true>(cd.nw, sv, b.ncr, A.sw, tile, lb);
+    uint32_t o = lb.o;
+    unsigned long long r = lb.r;
+    warp_min_key(o, r);
+    if (o != 0xffffffffu && (bseg < 0 || o < bo)) {
+      bo = o;
+      br = r;
+      bseg = s;
+    }
+  }
+  if (bseg >= 0) {
+    wn.found = 1;
+    wn.ii = ii;
+    wn.seg = bseg;
+    wn.rank = br;
+    wn.count = (I.branch == kBranchCpu) ? proc : I.total;
+    wn.cost = key_cost(bo);
+  }
+}
+
 __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
   __shared__ WarpArea areas[kTriageWarps];
   const int lane = threadIdx.x & 31;
@@ -383,7 +450,7 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
         }
       }
     }
-    if (lane < 32) A.sw[lane] = (lane < cd.nw) ? s_lane : 0u;
+    A.sw[lane] = (lane < cd.nw) ? s_lane : 0u;
     int ws = __popc(s_lane);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) ws += __shfl_xor_sync(kFull, ws, o);
@@ -401,7 +468,7 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
         for (int c = lane; c < cd.m; c += 32) b.dec_err[(size_t)shot * cd.m + c] = 0;
       if (b.dec_log && cd.family == kDem)
         for (int j = lane; j < cd.n_logicos; j += 32) b.dec_log[(size_t)shot * cd.n_logicos + j] = 0;
-      if (b.deferred) b.deferred[shot] = 0;
+      if (b.deferred && lane == 0) b.deferred[shot] = 0;
       __syncwarp();
       continue;
     }
@@ -433,90 +500,30 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
       J.code = ci;
       J.original_weight = original_weight;
       J.best = kNone;
-      J.chunks_done = 0;
+      J.tiles_done = 0;
     }
     __syncwarp();
 
-    // ---- light or heavy ------------------------------------------------------
-    unsigned long long total = 0;
-    bool light = true;
-    for (int ii = 0; ii < J.n_it; ++ii) {
-      total += J.it[ii].total;
-      if (J.it[ii].tam > kLightTam || J.it[ii].tam * cd.nwp > kLightWords) light = false;
-    }
-    if (total > (1ull << b.light_max_log2)) light = false;
+    // ---- iterations in upstream order; the first one over the light budget
+    //      and everything after it go to the search kernel ---------------------
     const bool ml = cd.variant == kMl;
-    const uint32_t *ebits = A.eb;
-
-    if (light) {
-      Winner wn;
-      wn.found = 0;
-      wn.ii = wn.seg = 0;
-      wn.rank = wn.count = 0;
-      wn.cost = 0.0f;
-      for (int ii = 0; ii < J.n_it && !wn.found; ++ii) {
-        IterInfo &I = J.it[ii];
-        stage_iteration(cd, A.am[I.src], I.tam, A.pos, A.tmp, A.cols, A.llr);
-        if (lane == 0) {
-          I.pos = A.pos;
-          I.cols = A.cols;
-          I.llr = A.llr;
-          if (ml) {
-            float pf = 0.0f;
-            I.prefix[0] = 0.0f;
-            for (int w = 1; w <= kMaxW; ++w) {
-              if (w <= I.tam) pf = __fadd_rn(pf, A.llr[w - 1]);
-              I.prefix[w] = pf;
-            }
-          }
-        }
-        __syncwarp();
-        if (!ml) {
-          for (int s = I.seg_lo; s < I.seg_hi && !wn.found; ++s) {
-            const Seg &S = J.seg[s];
-            if (S.dup) continue;
-            SegView sv{A.cols, A.llr, I.tam, S.w, S.K, cd.nwp, cd.nw, S.nprefix, S.base};
-            LaneBest lb;
-            lb.reset();
-            for (unsigned long long tile = 0; tile < S.ntiles; ++tile)
-              eval_dispatch<false>(cd.nw, sv, b.ncr, A.sw, tile, lb);
-            const unsigned long long g = warp_min_u64(lb.g);
-            if (g != kNone) wn = winner_from_index(J, g, cd.variant == kProb);
-          }
-        } else {
-          // upstream search_cpu_ml (grand_decoder.cu:620-656), one weight at a time
-          uint32_t bo = 0xffffffffu;
-          unsigned long long br = kNone, proc = 0;
-          int bseg = -1;
-          for (int s = I.seg_lo; s < I.seg_hi; ++s) {
-            const Seg &S = J.seg[s];
-            if (bseg >= 0 && I.prefix[S.w] >= key_cost(bo)) break;
-            proc += S.count;
-            SegView sv{A.cols, A.llr, I.tam, S.w, S.K, cd.nwp, cd.nw, S.nprefix, S.base};
-            LaneBest lb;
-            lb.reset();
-            for (unsigned long long tile = 0; tile < S.ntiles; ++tile)
-              eval_dispatch<true>(cd.nw, sv, b.ncr, A.sw, tile, lb);
-            uint32_t o = lb.o;
-            unsigned long long r = lb.r;
-            warp_min_key(o, r);
-            if (o != 0xffffffffu && (bseg < 0 || o < bo)) {
-              bo = o;
-              br = r;
-              bseg = s;
-            }
-          }
-          if (bseg >= 0) {
-            wn.found = 1;
-            wn.ii = ii;
-            wn.seg = bseg;
-            wn.rank = br;
-            wn.count = (I.branch == kBranchCpu) ? proc : I.total;
-            wn.cost = key_cost(bo);
-          }
-        }
+    const unsigned long long budget = 1ull << b.light_max_log2;
+    Winner wn;
+    wn.found = 0;
+    wn.ii = wn.seg = 0;
+    wn.rank = wn.count = 0;
+    wn.cost = 0.0f;
+    int heavy_from = -1;
+    for (int ii = 0; ii < J.n_it && !wn.found; ++ii) {
+      const IterInfo &I = J.it[ii];
+      if (I.total > budget || I.tam > kLightTam || I.tam * cd.nwp > kLightWords) {
+        heavy_from = ii;
+        break;
       }
-      finish_shot(b, cd, J, shot, wn, ebits, A.delta);
+      light_search(b, cd, J, A, ii, wn);
+    }
+    if (heavy_from < 0) {
+      finish_shot(b, cd, J, shot, wn, A.eb, A.delta);
       if (b.deferred && lane == 0) b.deferred[shot] = 0;
       __syncwarp();
       continue;
@@ -524,31 +531,37 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
 
     // ---- heavy: publish a Job ------------------------------------------------
     unsigned long long words = 0;
-    for (int ii = 0; ii < J.n_it; ++ii) {
+    for (int ii = heavy_from; ii < J.n_it; ++ii) {
       const unsigned long long tm = (unsigned long long)J.it[ii].tam;
-      words += (tm * cd.nwp + 3ull) & ~3ull;       // columns
+      words += (tm * cd.nwp + 3ull) & ~3ull;              // columns
       words += ((ml ? 2ull : 1ull) * tm + 3ull) & ~3ull;  // positions (+ sort buffer)
-      if (ml) words += (tm + 3ull) & ~3ull;        // LLRs
+      if (ml) words += (tm + 3ull) & ~3ull;               // LLRs
     }
     words += 128;  // supplied bits
-    unsigned long long off = 0, jslot = 0, cbase = 0, nch = 0;
+    unsigned long long off = 0, jslot = 0, tbase = 0, ntl = 0;
     int ok = 1;
     if (lane == 0) {
+      J.it_lo = heavy_from;
       for (int s = 0; s < J.nseg; ++s) {
         Seg &S = J.seg[s];
-        S.nchunks = S.dup ? 0ull : (S.ntiles + kTilesPerChunk - 1) / kTilesPerChunk;
-        S.chunk_lo = nch;
-        nch += S.nchunks;
+        S.njt = (S.dup || S.iter < heavy_from) ? 0ull : S.ntiles;
+        S.tile_lo = ntl;
+        ntl += S.njt;
       }
       off = atomicAdd(&b.counters[2], words);
-      if (off + words > b.scratch_words) ok = 0;
-      if (ok) {
-        const unsigned long long old = atomicAdd(&b.counters[0], (1ull << 40) | nch);
-        jslot = old >> 40;
-        cbase = old & ((1ull << 40) - 1ull);
-        if (jslot >= (unsigned long long)b.max_jobs) ok = 0;
+      if (off + words > b.scratch_words) {
+        ok = 0;
+        atomicOr(b.status, kStatusScratchOverflow);
       }
-      if (!ok) atomicOr(b.status, ok ? 0u : kStatusJobOverflow);
+      if (ok) {
+        const unsigned long long old = atomicAdd(&b.counters[0], (1ull << 40) | ntl);
+        jslot = old >> 40;
+        tbase = old & ((1ull << 40) - 1ull);
+        if (jslot >= (unsigned long long)b.max_jobs) {
+          ok = 0;
+          atomicOr(b.status, kStatusJobOverflow);
+        }
+      }
     }
     ok = __shfl_sync(kFull, ok, 0);
     if (!ok) {
@@ -558,10 +571,10 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
     }
     off = __shfl_sync(kFull, off, 0);
     jslot = __shfl_sync(kFull, jslot, 0);
-    cbase = __shfl_sync(kFull, cbase, 0);
-    nch = __shfl_sync(kFull, nch, 0);
+    tbase = __shfl_sync(kFull, tbase, 0);
+    ntl = __shfl_sync(kFull, ntl, 0);
     uint32_t *sp = b.scratch + off;
-    for (int ii = 0; ii < J.n_it; ++ii) {
+    for (int ii = heavy_from; ii < J.n_it; ++ii) {
       IterInfo &I = J.it[ii];
       const unsigned long long tm = (unsigned long long)I.tam;
       uint32_t *cols = sp;
@@ -591,11 +604,11 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
       __syncwarp();
     }
     for (int q = lane; q < 128; q += 32) sp[q] = A.eb[q];
-    for (int q = lane; q < kMaxRows / 32; q += 32) J.sw[q] = A.sw[q];
+    J.sw[lane] = A.sw[lane];
     if (lane == 0) {
       J.ebits = sp;
-      J.chunk_base = cbase;
-      J.nchunks = nch;
+      J.tile_base = tbase;
+      J.ntiles = ntl;
       for (int i = 0; i < kMaxIters; ++i)
         for (int w = 0; w <= kMaxW; ++w) J.mlkey[i][w][0] = J.mlkey[i][w][1] = kNone;
     }
@@ -611,9 +624,9 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
 }
 
 // ---------------------------------------------------------------------------
-// Kernel 2: persistent work-stealing search over the Jobs' chunks.
+// Kernel 2: persistent work-stealing search over the Jobs' tiles.
 // ---------------------------------------------------------------------------
-__device__ bool chunk_skip(const Job &J, const Seg &S, const IterInfo &I, bool ml) {
+__device__ bool tile_skip(const Job &J, const Seg &S, const IterInfo &I, bool ml) {
   if (!ml) {
     const unsigned long long best = *reinterpret_cast<const volatile unsigned long long *>(&J.best);
     return S.base >= best;
@@ -636,7 +649,7 @@ __device__ Winner winner_ml(const Job &J) {
   wn.ii = wn.seg = 0;
   wn.rank = wn.count = 0;
   wn.cost = 0.0f;
-  for (int ii = 0; ii < J.n_it; ++ii) {
+  for (int ii = J.it_lo; ii < J.n_it; ++ii) {
     const IterInfo &I = J.it[ii];
     uint32_t bo = 0xffffffffu;
     unsigned long long br = kNone, proc = 0;
@@ -666,113 +679,94 @@ __device__ Winner winner_ml(const Job &J) {
 }
 
 __global__ void __launch_bounds__(kSearchThreads) search_kernel(DevBatch b) {
-  __shared__ __align__(16) uint32_t s_cols[kStageWords];
-  __shared__ uint32_t s_sw[kMaxRows / 32];
-  __shared__ uint32_t s_delta[kMaxCols / 32];
-  __shared__ unsigned long long s_chunk;
-  __shared__ int s_job, s_seg, s_skip, s_final, st_job, st_it;
+  __shared__ __align__(16) uint32_t s_stage[kSearchWarps][kWarpStage];
+  __shared__ uint32_t s_sw[kSearchWarps][kMaxRows / 32];
+  __shared__ uint32_t s_delta[kSearchWarps][kMaxCols / 32];
 
-  const int tid = threadIdx.x;
-  const int lane = tid & 31;
-  const int warp = tid >> 5;
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  uint32_t *stage = s_stage[warp];
+  uint32_t *sw = s_sw[warp];
   const unsigned long long packed = *reinterpret_cast<volatile unsigned long long *>(b.counters);
   unsigned long long njobs = packed >> 40;
   unsigned long long total = packed & ((1ull << 40) - 1ull);
   if (njobs > (unsigned long long)b.max_jobs) {
     njobs = b.max_jobs;
-    total = njobs ? b.jobs[njobs - 1].chunk_base + b.jobs[njobs - 1].nchunks : 0ull;
+    total = njobs ? b.jobs[njobs - 1].tile_base + b.jobs[njobs - 1].ntiles : 0ull;
   }
-  if (tid == 0) st_job = -1;
+  int st_job = -1, st_it = -1;
 
   for (;;) {
-    if (tid == 0) {
-      const unsigned long long c = atomicAdd(&b.counters[1], 1ull);
-      s_chunk = c;
-      if (c < total) {
-        int lo = 0, hi = (int)njobs - 1;
-        while (lo < hi) {
-          const int mid = (lo + hi + 1) >> 1;
-          if (b.jobs[mid].chunk_base <= c) lo = mid;
-          else hi = mid - 1;
+    unsigned long long t0 = 0;
+    if (lane == 0) t0 = atomicAdd(&b.counters[1], (unsigned long long)kTilesPerFetch);
+    t0 = __shfl_sync(kFull, t0, 0);
+    if (t0 >= total) break;
+    const unsigned long long t1 = (t0 + kTilesPerFetch < total) ? t0 + kTilesPerFetch : total;
+    for (unsigned long long t = t0; t < t1; ++t) {
+      int lo = 0, hi = (int)njobs - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (b.jobs[mid].tile_base <= t) lo = mid;
+        else hi = mid - 1;
+      }
+      Job &J = b.jobs[lo];
+      const unsigned long long lt = t - J.tile_base;
+      int sg = 0;
+      while (sg < J.nseg - 1 &&
+             !(J.seg[sg].njt && lt >= J.seg[sg].tile_lo && lt < J.seg[sg].tile_lo + J.seg[sg].njt))
+        ++sg;
+      const Seg &S = J.seg[sg];
+      const IterInfo &I = J.it[S.iter];
+      const DevCode &cd = b.codes[J.code];
+      const bool ml = cd.variant == kMl;
+      if (!tile_skip(J, S, I, ml)) {
+        const bool staged = I.tam * cd.nwp <= kWarpStage;
+        if (st_job != lo || st_it != S.iter) {
+          __syncwarp();
+          if (staged) {
+            const uint4 *src = reinterpret_cast<const uint4 *>(I.cols);
+            uint4 *dst = reinterpret_cast<uint4 *>(stage);
+            const int n4 = (I.tam * cd.nwp + 3) / 4;
+            for (int i = lane; i < n4; i += 32) dst[i] = src[i];
+          }
+          sw[lane] = J.sw[lane];
+          __syncwarp();
+          st_job = lo;
+          st_it = S.iter;
         }
-        s_job = lo;
-        const Job &J = b.jobs[lo];
-        const unsigned long long lc = c - J.chunk_base;
-        int sg = 0;
-        while (sg < J.nseg - 1 &&
-               !(lc >= J.seg[sg].chunk_lo && lc < J.seg[sg].chunk_lo + J.seg[sg].nchunks))
-          ++sg;
-        s_seg = sg;
-        const DevCode &cd = b.codes[J.code];
-        s_skip = chunk_skip(J, J.seg[sg], J.it[J.seg[sg].iter], cd.variant == kMl) ? 1 : 0;
+        SegView sv{staged ? stage : I.cols, I.llr, I.tam, S.w, S.K, cd.nwp, cd.nw, S.nprefix,
+                   S.base};
+        LaneBest lb;
+        lb.reset();
+        if (ml) eval_dispatch<true>(cd.nw, sv, b.ncr, sw, lt - S.tile_lo, lb);
+        else eval_dispatch<false>(cd.nw, sv, b.ncr, sw, lt - S.tile_lo, lb);
+        if (!ml) {
+          const unsigned long long g = warp_min_u64(lb.g);
+          if (lane == 0 && g != kNone) atomicMin(&J.best, g);
+        } else {
+          uint32_t o = lb.o;
+          unsigned long long r = lb.r;
+          warp_min_key(o, r);
+          if (lane == 0 && o != 0xffffffffu)
+            if (!atomic_min_key(J.mlkey[S.iter][S.w], o, r)) atomicOr(b.status, kStatusCasLimit);
+        }
       }
-    }
-    __syncthreads();
-    if (s_chunk >= total) break;
-
-    Job &J = b.jobs[s_job];
-    const Seg &S = J.seg[s_seg];
-    const IterInfo &I = J.it[S.iter];
-    const DevCode &cd = b.codes[J.code];
-    const bool ml = cd.variant == kMl;
-    const bool staged = I.tam * cd.nwp <= kStageWords;
-
-    if (!s_skip && staged && (st_job != s_job || st_it != S.iter)) {
-      const uint4 *src = reinterpret_cast<const uint4 *>(I.cols);
-      uint4 *dst = reinterpret_cast<uint4 *>(s_cols);
-      const int n4 = (I.tam * cd.nwp + 3) / 4;
-      for (int i = tid; i < n4; i += kSearchThreads) dst[i] = src[i];
-      for (int i = tid; i < kMaxRows / 32; i += kSearchThreads) s_sw[i] = J.sw[i];
-      __syncthreads();
-      if (tid == 0) {
-        st_job = s_job;
-        st_it = S.iter;
+      int last = 0;
+      if (lane == 0) {
+        __threadfence();
+        last = (atomicAdd(&J.tiles_done, 1ull) + 1ull == J.ntiles) ? 1 : 0;
       }
-    } else if (!s_skip && !staged) {
-      for (int i = tid; i < kMaxRows / 32; i += kSearchThreads) s_sw[i] = J.sw[i];
-      if (tid == 0) st_job = -1;
-    }
-    __syncthreads();
-
-    if (!s_skip) {
-      const unsigned long long lc = s_chunk - J.chunk_base - S.chunk_lo;
-      const unsigned long long t0 = lc * kTilesPerChunk;
-      unsigned long long t1 = t0 + kTilesPerChunk;
-      if (t1 > S.ntiles) t1 = S.ntiles;
-      SegView sv{staged ? s_cols : I.cols, I.llr, I.tam, S.w, S.K, cd.nwp, cd.nw, S.nprefix,
-                 S.base};
-      LaneBest lb;
-      lb.reset();
-      for (unsigned long long tile = t0 + warp; tile < t1; tile += kSearchWarps) {
-        if (ml) eval_dispatch<true>(cd.nw, sv, b.ncr, s_sw, tile, lb);
-        else eval_dispatch<false>(cd.nw, sv, b.ncr, s_sw, tile, lb);
+      last = __shfl_sync(kFull, last, 0);
+      if (last) {
+        __threadfence();
+        Winner wn;
+        if (!ml)
+          wn = winner_from_index(J, *reinterpret_cast<volatile unsigned long long *>(&J.best),
+                                 cd.variant == kProb);
+        else
+          wn = winner_ml(J);
+        finish_shot(b, cd, J, J.shot, wn, J.ebits, s_delta[warp]);
       }
-      if (!ml) {
-        const unsigned long long g = warp_min_u64(lb.g);
-        if (lane == 0 && g != kNone) atomicMin(&J.best, g);
-      } else {
-        uint32_t o = lb.o;
-        unsigned long long r = lb.r;
-        warp_min_key(o, r);
-        if (lane == 0 && o != 0xffffffffu)
-          if (!atomic_min_key(J.mlkey[S.iter][S.w], o, r)) atomicOr(b.status, kStatusCasLimit);
-      }
-    }
-    __syncthreads();
-    if (tid == 0) {
-      __threadfence();
-      const unsigned long long d = atomicAdd(&J.chunks_done, 1ull);
-      s_final = (d + 1ull == J.nchunks) ? 1 : 0;
-    }
-    __syncthreads();
-    if (s_final && warp == 0) {
-      __threadfence();
-      Winner wn;
-      if (!ml)
-        wn = winner_from_index(J, *reinterpret_cast<volatile unsigned long long *>(&J.best),
-                               cd.variant == kProb);
-      else wn = winner_ml(J);
-      finish_shot(b, cd, J, J.shot, wn, J.ebits, s_delta);
     }
   }
 }
