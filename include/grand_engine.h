@@ -94,6 +94,11 @@ int grand_engine_kernel_times(GrandEngine *engine, void *stream, float *triage_m
  * in ops/s, the ceiling of the search kernel's integer roofline; < 0 on error. */
 double grand_measure_int_peak(void);
 
+/* Diagnostic: one line describing the current device as the library sees it
+ * (SM count, resident CTAs per SM of both kernels, whether the GPU can read
+ * pageable host memory directly).  Returns the length written or < 0. */
+int grand_device_info(char *buf, int len);
+
 #ifdef __cplusplus
 }
 #endif

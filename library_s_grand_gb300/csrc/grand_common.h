@@ -15,7 +15,7 @@
 
 #include <stdint.h>
 
-#include "../../include/grand_decoder.h"
+#include "grand_decoder.h"
 
 namespace grand {
 
@@ -59,7 +59,7 @@ struct DevCode {
   const int *colw;           // m
   const uint32_t *rows;      // R * mw (CSS, errors input)
   const uint32_t *rref;      // rank * mw
-  const int *piv;            // rank
+  const int *pivrow;         // m: RREF row whose pivot is column c, or -1
   const uint32_t *lcols;     // m * nlw
   const float *llr;          // m
 };
@@ -76,7 +76,9 @@ struct Seg {
   unsigned long long ntiles; // tiles of 32 lanes x K prefixes
   unsigned long long tile_lo;// first tile of this block within the job (search kernel)
   unsigned long long njt;    // tiles the search kernel runs for this block (0: none)
+  const unsigned long long *cum; // run tiles: tiles before run c, c = 0..tam-1 (scratch)
   int K;                     // prefixes per lane in a tile
+  int runs;                  // 1: register-blocked run tiles (w >= 3, nw <= 8); 0: colex tiles
 };
 
 struct IterInfo {

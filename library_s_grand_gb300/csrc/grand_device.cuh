@@ -258,6 +258,232 @@ __device__ __forceinline__ void eval_tile(const SegView &sv, const unsigned long
   }
 }
 
+// ---------------------------------------------------------------------------
+// Register-blocked tiles for weights >= 3 (NW = 1..8).
+//
+// The (w-1)-prefixes whose largest element is c form one contiguous colex run
+// of C(c, w-2) prefixes (their other w-2 elements are any subset of [0, c)).  A
+// run tile gives each lane KK consecutive prefixes of one run, so every prefix
+// in the warp has the same largest element: the warp walks j = c+1 .. tam-1 in
+// lockstep with no masking, loads column j once (shared-memory broadcast) and
+// compares it against the KK T vectors each lane keeps in registers.  Per
+// candidate that is NW XOR-OR word operations and half a 3-way minimum.
+// ---------------------------------------------------------------------------
+template <int NW>
+__device__ __forceinline__ void load_words(const uint32_t *col, uint32_t (&a)[NW]) {
+  if constexpr (NW == 1) {
+    a[0] = col[0];
+  } else if constexpr (NW == 2) {
+    uint2 v = *reinterpret_cast<const uint2 *>(col);
+    a[0] = v.x; a[1] = v.y;
+  } else if constexpr (NW <= 4) {
+    uint4 v = *reinterpret_cast<const uint4 *>(col);
+    a[0] = v.x; a[1] = v.y; a[2] = v.z;
+    if constexpr (NW == 4) a[3] = v.w;
+  } else {
+    uint4 v = *reinterpret_cast<const uint4 *>(col);
+    uint4 u = *reinterpret_cast<const uint4 *>(col + 4);
+    a[0] = v.x; a[1] = v.y; a[2] = v.z; a[3] = v.w; a[4] = u.x;
+    if constexpr (NW >= 6) a[5] = u.y;
+    if constexpr (NW >= 7) a[6] = u.z;
+    if constexpr (NW >= 8) a[7] = u.w;
+  }
+}
+
+template <int NW>
+__device__ __forceinline__ uint32_t diff_words(const uint32_t (&a)[NW], const uint32_t (&T)[NW]) {
+  uint32_t z = a[0] ^ T[0];
+#pragma unroll
+  for (int i = 1; i < NW; ++i) z |= a[i] ^ T[i];
+  return z;
+}
+
+// Colex successor of an ascending kk-subset y of [0, c); returns the highest
+// changed position (elements 0..adv changed), -1 when exhausted.
+__device__ __forceinline__ int colex_next(int (&y)[5], int kk, int c) {
+  int adv = -1;
+#pragma unroll
+  for (int i = 0; i < 5; ++i) {
+    if (i < kk && adv < 0) {
+      int lim = c;
+      if (i + 1 < 5 && i + 1 < kk) lim = y[(i + 1) < 5 ? i + 1 : 4];
+      if (y[i] + 1 < lim) adv = i;
+    }
+  }
+  if (adv >= 0) {
+#pragma unroll
+    for (int i = 0; i < 5; ++i)
+      if (i < kk && i <= adv) y[i] = (i == adv) ? y[i] + 1 : i;
+  }
+  return adv;
+}
+
+// Colex unranking of a kk-subset of [0, c): closed forms for kk <= 2 (weights 3
+// and 4, the common case), the binomial-table search otherwise.
+__device__ __forceinline__ void sub_unrank(const unsigned long long *t, unsigned long long r,
+                                           int kk, int c, int (&y)[5]) {
+  if (kk == 1) {
+    y[0] = (int)r;
+  } else if (kk == 2) {
+    // largest v with v(v-1)/2 <= r, from the float square root then corrected
+    int v = (int)((1.0f + sqrtf(1.0f + 8.0f * (float)r)) * 0.5f);
+    if (v < 1) v = 1;
+    while ((unsigned long long)v * (v - 1) / 2 > r) --v;
+    while ((unsigned long long)(v + 1) * v / 2 <= r) ++v;
+    y[1] = v;
+    y[0] = (int)(r - (unsigned long long)v * (v - 1) / 2);
+  } else {
+    colex_unrank(t, r, kk, c - 1, y);
+  }
+}
+
+// Colex successor inside a run (the caller only asks for existing successors).
+__device__ __forceinline__ int sub_next(int (&y)[5], int kk, int c) {
+  if (kk == 1) {
+    ++y[0];
+    return 0;
+  }
+  if (kk == 2) {
+    if (y[0] + 1 < y[1]) {
+      ++y[0];
+      return 0;
+    }
+    ++y[1];
+    y[0] = 0;
+    return 1;
+  }
+  return colex_next(y, kk, c);
+}
+
+template <int NW>
+__device__ __forceinline__ void prefix_T(const uint32_t *cols, int nwp, const uint32_t (&base)[NW],
+                                         const int (&y)[5], int kk, uint32_t (&T)[NW]) {
+#pragma unroll
+  for (int i = 0; i < NW; ++i) T[i] = base[i];
+#pragma unroll
+  for (int e = 0; e < 5; ++e)
+    if (e < kk) {
+      uint32_t a[NW];
+      load_words<NW>(cols + (size_t)y[e] * nwp, a);
+#pragma unroll
+      for (int i = 0; i < NW; ++i) T[i] ^= a[i];
+    }
+}
+
+// One run tile: run c, lane l takes prefixes r0 + l*KK + [0, KK) of the run.
+template <int NW, int KK, bool ML>
+__device__ __forceinline__ void eval_run_tile(const SegView &sv, const unsigned long long *t,
+                                              const uint32_t *sw, int c, unsigned long long r0,
+                                              LaneBest &lb) {
+  constexpr int nwp = Words<NW>::nwp;
+  const int lane = threadIdx.x & 31;
+  const int k = sv.w - 1;   // prefix length (>= 2)
+  const int kk = k - 1;     // elements below c (>= 1)
+  const int tam = sv.tam;
+  const uint32_t *cols = sv.cols;
+  const unsigned long long run = ncr(t, c, kk);
+  const unsigned long long r = r0 + (unsigned long long)lane * KK;
+  const int v = r >= run ? 0 : (int)((run - r) < (unsigned long long)KK ? (run - r) : KK);
+
+  uint32_t base[NW];
+  {
+    uint32_t a[NW];
+    load_words<NW>(cols + (size_t)c * nwp, a);
+#pragma unroll
+    for (int i = 0; i < NW; ++i) base[i] = sw[i] ^ a[i];
+  }
+  int y[5] = {0, 1, 2, 3, 4};
+  if (v > 0) sub_unrank(t, r, kk, c, y);
+  uint32_t T[KK][NW];
+  prefix_T<NW>(cols, nwp, base, y, kk, T[0]);
+#pragma unroll
+  for (int s = 1; s < KK; ++s) {
+#pragma unroll
+    for (int i = 0; i < NW; ++i) T[s][i] = T[s - 1][i];
+    if (s < v) {
+      int old[5];
+#pragma unroll
+      for (int e = 0; e < 5; ++e) old[e] = y[e];
+      const int adv = sub_next(y, kk, c);
+#pragma unroll
+      for (int e = 0; e < 5; ++e)
+        if (e < kk && e <= adv && old[e] != y[e]) {
+          uint32_t a[NW], b2[NW];
+          load_words<NW>(cols + (size_t)old[e] * nwp, a);
+          load_words<NW>(cols + (size_t)y[e] * nwp, b2);
+#pragma unroll
+          for (int i = 0; i < NW; ++i) T[s][i] ^= a[i] ^ b2[i];
+        }
+    } else {
+#pragma unroll
+      for (int i = 0; i < NW; ++i) T[s][i] = T[0][i];
+    }
+  }
+
+  uint32_t acc = 0xffffffffu;
+#pragma unroll 2
+  for (int j = c + 1; j < tam; ++j) {
+    uint32_t a[NW];
+    load_words<NW>(cols + (size_t)j * nwp, a);
+    if constexpr (KK == 4) {
+      const uint32_t z0 = diff_words<NW>(a, T[0]);
+      const uint32_t z1 = diff_words<NW>(a, T[1]);
+      const uint32_t z2 = diff_words<NW>(a, T[2]);
+      const uint32_t z3 = diff_words<NW>(a, T[3]);
+      acc = __vimin3_u32(acc, z0, z1);
+      acc = __vimin3_u32(acc, z2, z3);
+    } else {
+#pragma unroll
+      for (int s = 0; s < KK; ++s) acc = min(acc, diff_words<NW>(a, T[s]));
+    }
+  }
+
+  if (v > 0 && acc == 0u) {
+    // At least one of this lane's prefixes has a match: find them all (rare).
+    int yy[5] = {0, 1, 2, 3, 4};
+    sub_unrank(t, r, kk, c, yy);
+    for (int s = 0; s < v; ++s) {
+      if (s > 0) sub_next(yy, kk, c);
+      uint32_t Ts[NW];
+      prefix_T<NW>(cols, nwp, base, yy, kk, Ts);
+      int x[5];
+#pragma unroll
+      for (int e = 0; e < 5; ++e) x[e] = (e < kk) ? yy[e] : (e == kk ? c : 0);
+      float pc = 0.0f;
+      if constexpr (ML) {
+#pragma unroll
+        for (int e = 0; e < 5; ++e)
+          if (e < k) pc = __fadd_rn(pc, sv.llr[x[e]]);
+      }
+      for (int j = c + 1; j < tam; ++j) {
+        uint32_t a[NW];
+        load_words<NW>(cols + (size_t)j * nwp, a);
+        if (diff_words<NW>(a, Ts) != 0u) continue;
+        const unsigned long long rk = lex_rank(t, tam, sv.w, x, k, j);
+        if constexpr (!ML) {
+          const unsigned long long g = sv.base + rk;
+          if (g < lb.g) lb.g = g;
+          break;
+        } else {
+          const uint32_t o = cost_key(__fadd_rn(pc, sv.llr[j]));
+          if (o < lb.o || (o == lb.o && rk < lb.r)) {
+            lb.o = o;
+            lb.r = rk;
+          }
+        }
+      }
+    }
+  }
+}
+
+// Number of run tiles of run c for weight w (KK prefixes per lane).
+__device__ __forceinline__ unsigned long long run_tiles(const unsigned long long *t, int c, int w,
+                                                        int KK) {
+  const unsigned long long n = ncr(t, c, w - 2);
+  const unsigned long long per = 32ull * (unsigned long long)KK;
+  return (n + per - 1ull) / per;
+}
+
 __device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {

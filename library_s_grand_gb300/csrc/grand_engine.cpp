@@ -1,5 +1,5 @@
 // grand_engine.cpp -- batched mixed-code decoding (include/grand_engine.h).
-#include "../../include/grand_engine.h"
+#include "grand_engine.h"
 
 #include <math.h>
 #include <stdio.h>
@@ -382,6 +382,18 @@ int grand_engine_kernel_times(GrandEngine *e, void *stream, float *triage_ms, fl
   if (triage_ms) *triage_ms = a;
   if (search_ms) *search_ms = b;
   return 0;
+}
+
+int grand_device_info(char *buf, int len) {
+  int err = 0;
+  Context *ctx = Context::get(&err);
+  if (!ctx) return err;
+  if (!buf || len <= 0) return GRAND_ERR_INVALID;
+  return snprintf(buf, (size_t)len,
+                  "device=%d sms=%d triage_ctas_per_sm=%d search_ctas_per_sm=%d "
+                  "pageable_memory_access=%d",
+                  ctx->device, ctx->sm_count, ctx->triage_bps, ctx->search_bps,
+                  ctx->pageable_access);
 }
 
 double grand_measure_int_peak(void) {

@@ -60,7 +60,7 @@ CodeTables::~CodeTables() {
   cudaFree(cols);
   cudaFree(colw);
   cudaFree(rref);
-  cudaFree(piv);
+  cudaFree(pivrow);
   cudaFree(lcols);
 }
 
@@ -255,8 +255,10 @@ std::shared_ptr<CodeTables> Context::tables(int family, const int *H, const int 
     std::vector<int> piv;
     t->rank = rref_bits(rows, n, t->mw, m, piv);
     rows.resize((size_t)t->rank * t->mw);
+    std::vector<int> pivrow(m, -1);
+    for (int r = 0; r < t->rank; ++r) pivrow[piv[r]] = r;
     e = upload(&t->rref, rows);
-    if (e == cudaSuccess) e = upload(&t->piv, piv);
+    if (e == cudaSuccess) e = upload(&t->pivrow, pivrow);
   }
   if (e == cudaSuccess && family == kDem) {
     std::vector<uint32_t> lc((size_t)m * std::max(t->nlw, 1), 0u);
@@ -312,7 +314,7 @@ DevCode make_devcode(const CodeTables &t, const CallParams &p) {
   d.colw = t.colw;
   d.rows = nullptr;
   d.rref = t.rref;
-  d.piv = t.piv;
+  d.pivrow = t.pivrow;
   d.lcols = t.lcols;
   d.llr = p.d_llr;
   return d;

@@ -29,7 +29,7 @@ struct CodeTables {
   uint32_t *cols = nullptr;
   int *colw = nullptr;
   uint32_t *rref = nullptr;
-  int *piv = nullptr;
+  int *pivrow = nullptr;
   uint32_t *lcols = nullptr;
   std::vector<int> key;  // exact content the tables were built from
   size_t bytes = 0;

@@ -31,7 +31,9 @@ constexpr int kLightWords = kLightTam * 8;
 constexpr int kSearchThreads = 256;
 constexpr int kSearchWarps = kSearchThreads / 32;
 constexpr int kWarpStage = 1280;  // staged active-column words per search warp
-constexpr int kTilesPerFetch = 2;
+constexpr int kTilesPerFetch = 4;
+constexpr int kRunKK = 8;       // prefixes per lane in a run tile (search kernel)
+constexpr int kRunKKLight = 4;  // the same inside the triage warp's light search
 
 struct alignas(16) WarpArea {
   uint32_t cols[kLightWords];
@@ -47,21 +49,28 @@ struct alignas(16) WarpArea {
 
 // ---------------------------------------------------------------------------
 // Planning: the threshold iterations and their weight blocks (lane 0 only).
+// The planner is resumable: each call walks upstream's iteration loop
+// (grand_decoder.cu:1284-1343) to the next iteration that is searched, appends
+// it and its weight blocks to the Job and returns 1, or records the outcome
+// fields of an exhausted loop and returns 0.  Shots usually resolve in their
+// first searched iteration, so later iterations are only planned when needed.
 // ---------------------------------------------------------------------------
-__device__ void plan_shot(const DevCode &cd, const unsigned long long *t, const int (&tam_raw)[3],
-                          int L, int tile_k, Job &J) {
-  J.n_it = 0;
-  J.nseg = 0;
-  J.failed = 0;
-  int tam = 0, tam_old = 0, passes = 0;
-  unsigned long long gbase = 0;
-  for (int i = 0; i < L; ++i) {
-    passes = i + 1;
-    tam = tam_raw[i];
+struct PlanState {
+  int i, tam, tam_old, passes;
+  unsigned long long gbase;
+};
+
+__device__ int plan_next(const DevCode &cd, const unsigned long long *t, const int (&tam_raw)[3],
+                         int L, int tile_k, Job &J, PlanState &P) {
+  while (P.i < L) {
+    const int i = P.i++;
+    P.passes = i + 1;
+    int tam = tam_raw[i];
     if (cd.family == kDem) {  // grand_decoder.cu:1550-1554
-      if (tam > cd.cap) tam = tam_old;
-      else tam_old = tam;
+      if (tam > cd.cap) tam = P.tam_old;
+      else P.tam_old = tam;
     }
+    P.tam = tam;
     if (tam <= 0) continue;
     const bool gpu = (tam > cd.thr && tam <= cd.cap && cd.mode == 1) || cd.mode == 0;
     const bool cpu = !gpu && ((tam <= cd.thr && cd.mode == 1) || cd.mode == -1);
@@ -76,7 +85,7 @@ __device__ void plan_shot(const DevCode &cd, const unsigned long long *t, const 
     I.branch = gpu ? kBranchGpu : kBranchCpu;
     I.src = i;
     I.seg_lo = J.nseg;
-    I.base = gbase;
+    I.base = P.gbase;
     I.phase_end[0] = I.phase_end[1] = I.phase_end[2] = 0;
     unsigned long long tot = 0;
     int wl[kMaxSegsPerIter], ph[kMaxSegsPerIter], nwl = 0;
@@ -105,10 +114,13 @@ __device__ void plan_shot(const DevCode &cd, const unsigned long long *t, const 
       S.dup = (seen >> S.w) & 1u;
       seen |= 1u << S.w;
       S.count = ncr(t, tam, S.w);
-      S.base = gbase + tot;
+      S.base = P.gbase + tot;
       S.nprefix = ncr(t, tam - 1, S.w - 1);
-      S.K = S.w <= 2 ? 1 : tile_k;
-      S.ntiles = (S.nprefix + 32ull * S.K - 1) / (32ull * S.K);
+      S.runs = (S.w >= 3 && cd.nw <= 8) ? 1 : 0;
+      S.cum = nullptr;
+      S.K = S.runs ? kRunKK : (S.w <= 2 ? 1 : tile_k);
+      // run-tile counts are built by the warp when a Job is published
+      S.ntiles = S.runs ? 0ull : (S.nprefix + 32ull * S.K - 1) / (32ull * S.K);
       tot += S.count;
       if (cd.variant == kProb) I.phase_end[S.phase] = tot;
     }
@@ -117,11 +129,13 @@ __device__ void plan_shot(const DevCode &cd, const unsigned long long *t, const 
         if (I.phase_end[k] < I.phase_end[k - 1]) I.phase_end[k] = I.phase_end[k - 1];
     I.seg_hi = J.nseg;
     I.total = tot;
-    gbase += tot;
+    P.gbase += tot;
     J.n_it++;
+    return 1;
   }
-  J.final_iteration = passes;
-  J.final_tam = tam;
+  J.final_iteration = P.passes;
+  J.final_tam = P.tam;
+  return 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -170,17 +184,26 @@ __device__ void finish_shot(const DevBatch &b, const DevCode &cd, const Job &J, 
     is_equal = __all_sync(kFull, eq) ? 1 : 0;
     __syncwarp();
     // degenerate: (e ^ e_est) in the row space of the other matrix
-    // (grand_decoder.cu:456-474).  In reduced row echelon form the pivot bits of
-    // the vector decide alone which rows are added.
-    bool ok = true;
-    for (int q = lane; q < cd.mw; q += 32) {
-      uint32_t acc = 0;
-      for (int r = 0; r < cd.rank; ++r) {
-        const int pc = __ldg(cd.piv + r);
-        if ((delta[pc >> 5] >> (pc & 31)) & 1u) acc ^= __ldg(cd.rref + (size_t)r * cd.mw + q);
+    // (grand_decoder.cu:456-474).  In reduced row echelon form the vector's own
+    // bits at pivot columns decide alone which rows upstream adds, so the test
+    // is delta == XOR of the rows pivoted on delta's set bits.
+    uint32_t acc[4] = {0u, 0u, 0u, 0u};  // words lane, lane+32, lane+64, lane+96
+    for (int q = 0; q < cd.mw; ++q) {
+      uint32_t word = delta[q];
+      while (word) {
+        const int c = q * 32 + __ffs(word) - 1;
+        word &= word - 1u;
+        const int r = __ldg(cd.pivrow + c);
+        if (r < 0) continue;
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+          if (lane + 32 * k < cd.mw) acc[k] ^= __ldg(cd.rref + (size_t)r * cd.mw + lane + 32 * k);
       }
-      ok = ok && acc == delta[q];
     }
+    bool ok = true;
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (lane + 32 * k < cd.mw) ok = ok && acc[k] == delta[lane + 32 * k];
     degenerate = __all_sync(kFull, ok) ? 1 : 0;
   } else if (wn.found && cd.family == kDem) {
     // decoded logical flips vs the supplied true flips (grand_decoder.cu:1623-1644)
@@ -328,6 +351,39 @@ __device__ __forceinline__ void eval_dispatch(int nw, const SegView &sv,
   }
 }
 
+template <bool ML, int KK>
+__device__ __forceinline__ void eval_run_dispatch(int nw, const SegView &sv,
+                                                  const unsigned long long *t, const uint32_t *sw,
+                                                  int c, unsigned long long r0, LaneBest &lb) {
+  switch (nw) {
+    case 1: eval_run_tile<1, KK, ML>(sv, t, sw, c, r0, lb); break;
+    case 2: eval_run_tile<2, KK, ML>(sv, t, sw, c, r0, lb); break;
+    case 3: eval_run_tile<3, KK, ML>(sv, t, sw, c, r0, lb); break;
+    case 4: eval_run_tile<4, KK, ML>(sv, t, sw, c, r0, lb); break;
+    case 5: eval_run_tile<5, KK, ML>(sv, t, sw, c, r0, lb); break;
+    case 6: eval_run_tile<6, KK, ML>(sv, t, sw, c, r0, lb); break;
+    case 7: eval_run_tile<7, KK, ML>(sv, t, sw, c, r0, lb); break;
+    default: eval_run_tile<8, KK, ML>(sv, t, sw, c, r0, lb); break;
+  }
+}
+
+// Every tile of one weight block, in order, by one warp (light path).
+template <bool ML>
+__device__ void eval_segment(const DevCode &cd, const SegView &sv, const Seg &S,
+                             const unsigned long long *t, const uint32_t *sw, LaneBest &lb) {
+  if (S.runs) {
+    const unsigned long long per = 32ull * kRunKKLight;
+    for (int c = S.w - 2; c <= sv.tam - 2; ++c) {
+      const unsigned long long nt = run_tiles(t, c, S.w, kRunKKLight);
+      for (unsigned long long q = 0; q < nt; ++q)
+        eval_run_dispatch<ML, kRunKKLight>(cd.nw, sv, t, sw, c, q * per, lb);
+    }
+  } else {
+    for (unsigned long long tile = 0; tile < S.ntiles; ++tile)
+      eval_dispatch<ML>(cd.nw, sv, t, sw, tile, lb);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Kernel 1: triage + light search.
 // ---------------------------------------------------------------------------
@@ -358,8 +414,7 @@ __device__ void light_search(const DevBatch &b, const DevCode &cd, Job &J, WarpA
       SegView sv{A.cols, A.llr, I.tam, S.w, S.K, cd.nwp, cd.nw, S.nprefix, S.base};
       LaneBest lb;
       lb.reset();
-      for (unsigned long long tile = 0; tile < S.ntiles; ++tile)
-        eval_dispatch<false>(cd.nw, sv, b.ncr, A.sw, tile, lb);
+      eval_segment<false>(cd, sv, S, b.ncr, A.sw, lb);
       const unsigned long long g = warp_min_u64(lb.g);
       if (g != kNone) wn = winner_from_index(J, g, cd.variant == kProb);
     }
@@ -376,8 +431,7 @@ __device__ void light_search(const DevBatch &b, const DevCode &cd, Job &J, WarpA
     SegView sv{A.cols, A.llr, I.tam, S.w, S.K, cd.nwp, cd.nw, S.nprefix, S.base};
     LaneBest lb;
     lb.reset();
-    for (unsigned long long tile = 0; tile < S.ntiles; ++tile)
-      eval_dispatch<true>(cd.nw, sv, b.ncr, A.sw, tile, lb);
+    eval_segment<true>(cd, sv, S, b.ncr, A.sw, lb);
     uint32_t o = lb.o;
     unsigned long long r = lb.r;
     warp_min_key(o, r);
@@ -494,15 +548,25 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
         tam_raw[i] += __popc(bits);
       }
     }
+    __shared__ PlanState plans[kTriageWarps];
+    PlanState &P = plans[wib];
     if (lane == 0) {
-      plan_shot(cd, b.ncr, tam_raw, L, b.tile_k, J);
+      J.n_it = 0;
+      J.nseg = 0;
+      J.failed = 0;
+      J.final_iteration = 0;
+      J.final_tam = 0;
+      P.i = 0;
+      P.tam = 0;
+      P.tam_old = 0;
+      P.passes = 0;
+      P.gbase = 0;
       J.shot = shot;
       J.code = ci;
       J.original_weight = original_weight;
       J.best = kNone;
       J.tiles_done = 0;
     }
-    __syncwarp();
 
     // ---- iterations in upstream order; the first one over the light budget
     //      and everything after it go to the search kernel ---------------------
@@ -514,13 +578,24 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
     wn.rank = wn.count = 0;
     wn.cost = 0.0f;
     int heavy_from = -1;
-    for (int ii = 0; ii < J.n_it && !wn.found; ++ii) {
+    for (;;) {
+      int more = 0;
+      if (lane == 0) more = plan_next(cd, b.ncr, tam_raw, L, b.tile_k, J, P);
+      more = __shfl_sync(kFull, more, 0);
+      __syncwarp();
+      if (!more) break;
+      const int ii = J.n_it - 1;
       const IterInfo &I = J.it[ii];
       if (I.total > budget || I.tam > kLightTam || I.tam * cd.nwp > kLightWords) {
         heavy_from = ii;
+        if (lane == 0)
+          while (plan_next(cd, b.ncr, tam_raw, L, b.tile_k, J, P)) {
+          }
+        __syncwarp();
         break;
       }
       light_search(b, cd, J, A, ii, wn);
+      if (wn.found) break;
     }
     if (heavy_from < 0) {
       finish_shot(b, cd, J, shot, wn, A.eb, A.delta);
@@ -537,30 +612,19 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
       words += ((ml ? 2ull : 1ull) * tm + 3ull) & ~3ull;  // positions (+ sort buffer)
       if (ml) words += (tm + 3ull) & ~3ull;               // LLRs
     }
+    for (int s = 0; s < J.nseg; ++s) {
+      const Seg &S = J.seg[s];
+      if (S.runs && !S.dup && S.iter >= heavy_from)
+        words += (2ull * (unsigned long long)J.it[S.iter].tam + 3ull) & ~3ull;  // run-tile table
+    }
     words += 128;  // supplied bits
     unsigned long long off = 0, jslot = 0, tbase = 0, ntl = 0;
     int ok = 1;
     if (lane == 0) {
-      J.it_lo = heavy_from;
-      for (int s = 0; s < J.nseg; ++s) {
-        Seg &S = J.seg[s];
-        S.njt = (S.dup || S.iter < heavy_from) ? 0ull : S.ntiles;
-        S.tile_lo = ntl;
-        ntl += S.njt;
-      }
       off = atomicAdd(&b.counters[2], words);
       if (off + words > b.scratch_words) {
         ok = 0;
         atomicOr(b.status, kStatusScratchOverflow);
-      }
-      if (ok) {
-        const unsigned long long old = atomicAdd(&b.counters[0], (1ull << 40) | ntl);
-        jslot = old >> 40;
-        tbase = old & ((1ull << 40) - 1ull);
-        if (jslot >= (unsigned long long)b.max_jobs) {
-          ok = 0;
-          atomicOr(b.status, kStatusJobOverflow);
-        }
       }
     }
     ok = __shfl_sync(kFull, ok, 0);
@@ -570,9 +634,6 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
       continue;
     }
     off = __shfl_sync(kFull, off, 0);
-    jslot = __shfl_sync(kFull, jslot, 0);
-    tbase = __shfl_sync(kFull, tbase, 0);
-    ntl = __shfl_sync(kFull, ntl, 0);
     uint32_t *sp = b.scratch + off;
     for (int ii = heavy_from; ii < J.n_it; ++ii) {
       IterInfo &I = J.it[ii];
@@ -603,6 +664,57 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
       }
       __syncwarp();
     }
+    // run-tile tables: cum[c] = run tiles before run c (warp prefix scan)
+    for (int sgi = 0; sgi < J.nseg; ++sgi) {
+      Seg &S = J.seg[sgi];
+      if (!S.runs || S.dup || S.iter < heavy_from) continue;
+      const int tam = J.it[S.iter].tam;
+      unsigned long long *cum = reinterpret_cast<unsigned long long *>(sp);
+      sp += (2ull * (unsigned long long)tam + 3ull) & ~3ull;
+      unsigned long long carry = 0;
+      for (int c0 = 0; c0 < tam; c0 += 32) {
+        const int c = c0 + lane;
+        const unsigned long long nt = (c <= tam - 2) ? run_tiles(b.ncr, c, S.w, kRunKK) : 0ull;
+        unsigned long long incl = nt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const unsigned long long u = __shfl_up_sync(kFull, incl, o);
+          if (lane >= o) incl += u;
+        }
+        if (c < tam) cum[c] = carry + incl - nt;
+        carry += __shfl_sync(kFull, incl, 31);
+      }
+      if (lane == 0) {
+        S.cum = cum;
+        S.ntiles = carry;
+      }
+      __syncwarp();
+    }
+    if (lane == 0) {
+      J.it_lo = heavy_from;
+      for (int sgi = 0; sgi < J.nseg; ++sgi) {
+        Seg &S = J.seg[sgi];
+        S.njt = (S.dup || S.iter < heavy_from) ? 0ull : S.ntiles;
+        S.tile_lo = ntl;
+        ntl += S.njt;
+      }
+      const unsigned long long old = atomicAdd(&b.counters[0], (1ull << 40) | ntl);
+      jslot = old >> 40;
+      tbase = old & ((1ull << 40) - 1ull);
+      if (jslot >= (unsigned long long)b.max_jobs) {
+        ok = 0;
+        atomicOr(b.status, kStatusJobOverflow);
+      }
+    }
+    ok = __shfl_sync(kFull, ok, 0);
+    if (!ok) {
+      if (lane == 0 && b.deferred) b.deferred[shot] = 1;
+      __syncwarp();
+      continue;
+    }
+    jslot = __shfl_sync(kFull, jslot, 0);
+    tbase = __shfl_sync(kFull, tbase, 0);
+    ntl = __shfl_sync(kFull, ntl, 0);
     for (int q = lane; q < 128; q += 32) sp[q] = A.eb[q];
     J.sw[lane] = A.sw[lane];
     if (lane == 0) {
@@ -678,7 +790,7 @@ __device__ Winner winner_ml(const Job &J) {
   return wn;
 }
 
-__global__ void __launch_bounds__(kSearchThreads) search_kernel(DevBatch b) {
+__global__ void __launch_bounds__(kSearchThreads, 3) search_kernel(DevBatch b) {
   __shared__ __align__(16) uint32_t s_stage[kSearchWarps][kWarpStage];
   __shared__ uint32_t s_sw[kSearchWarps][kMaxRows / 32];
   __shared__ uint32_t s_delta[kSearchWarps][kMaxCols / 32];
@@ -695,6 +807,15 @@ __global__ void __launch_bounds__(kSearchThreads) search_kernel(DevBatch b) {
     total = njobs ? b.jobs[njobs - 1].tile_base + b.jobs[njobs - 1].ntiles : 0ull;
   }
   int st_job = -1, st_it = -1;
+  // per-warp caches of the last job / weight block / run looked up, and a
+  // register copy of the current weight block's parameters
+  int cj = -1, cs = -1, cc = -1;
+  unsigned long long cj_lo = 0, cj_hi = 0, cs_lo = 0, cs_hi = 0, cc_lo = 0, cc_hi = 0;
+  Job *Jp = nullptr;
+  const DevCode *cdp = nullptr;
+  SegView sv{};
+  int s_runs = 0, s_iter = 0, s_ml = 0, s_prob = 0, s_nw = 0;
+  const unsigned long long *s_cum = nullptr;
 
   for (;;) {
     unsigned long long t0 = 0;
@@ -702,70 +823,131 @@ __global__ void __launch_bounds__(kSearchThreads) search_kernel(DevBatch b) {
     t0 = __shfl_sync(kFull, t0, 0);
     if (t0 >= total) break;
     const unsigned long long t1 = (t0 + kTilesPerFetch < total) ? t0 + kTilesPerFetch : total;
+    bool skip_known = false, skip = false;
+    unsigned long long pending = 0;
+    bool fenced = false;
     for (unsigned long long t = t0; t < t1; ++t) {
-      int lo = 0, hi = (int)njobs - 1;
-      while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (b.jobs[mid].tile_base <= t) lo = mid;
-        else hi = mid - 1;
+      if (cj < 0 || t < cj_lo || t >= cj_hi) {
+        int lo = 0, hi = (int)njobs - 1;
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (b.jobs[mid].tile_base <= t) lo = mid;
+          else hi = mid - 1;
+        }
+        cj = lo;
+        Jp = &b.jobs[lo];
+        cdp = &b.codes[Jp->code];
+        cj_lo = Jp->tile_base;
+        cj_hi = cj_lo + Jp->ntiles;
+        cs = -1;
       }
-      Job &J = b.jobs[lo];
-      const unsigned long long lt = t - J.tile_base;
-      int sg = 0;
-      while (sg < J.nseg - 1 &&
-             !(J.seg[sg].njt && lt >= J.seg[sg].tile_lo && lt < J.seg[sg].tile_lo + J.seg[sg].njt))
-        ++sg;
-      const Seg &S = J.seg[sg];
-      const IterInfo &I = J.it[S.iter];
-      const DevCode &cd = b.codes[J.code];
-      const bool ml = cd.variant == kMl;
-      if (!tile_skip(J, S, I, ml)) {
-        const bool staged = I.tam * cd.nwp <= kWarpStage;
-        if (st_job != lo || st_it != S.iter) {
+      Job &J = *Jp;
+      const unsigned long long lt = t - cj_lo;
+      if (cs < 0 || lt < cs_lo || lt >= cs_hi) {
+        int sg = 0;
+        while (sg < J.nseg - 1 &&
+               !(J.seg[sg].njt && lt >= J.seg[sg].tile_lo && lt < J.seg[sg].tile_lo + J.seg[sg].njt))
+          ++sg;
+        const Seg &S = J.seg[sg];
+        const IterInfo &I = J.it[S.iter];
+        cs = sg;
+        cs_lo = S.tile_lo;
+        cs_hi = cs_lo + S.njt;
+        cc = -1;
+        s_runs = S.runs;
+        s_cum = S.cum;
+        s_iter = S.iter;
+        s_nw = cdp->nw;
+        s_ml = cdp->variant == kMl;
+        s_prob = cdp->variant == kProb;
+        const bool staged = I.tam * cdp->nwp <= kWarpStage;
+        sv = SegView{staged ? stage : I.cols, I.llr, I.tam, S.w, S.K, cdp->nwp, cdp->nw,
+                     S.nprefix, S.base};
+        if (st_job != cj || st_it != S.iter) {
           __syncwarp();
           if (staged) {
             const uint4 *src = reinterpret_cast<const uint4 *>(I.cols);
             uint4 *dst = reinterpret_cast<uint4 *>(stage);
-            const int n4 = (I.tam * cd.nwp + 3) / 4;
+            const int n4 = (I.tam * cdp->nwp + 3) / 4;
             for (int i = lane; i < n4; i += 32) dst[i] = src[i];
           }
           sw[lane] = J.sw[lane];
           __syncwarp();
-          st_job = lo;
+          st_job = cj;
           st_it = S.iter;
         }
-        SegView sv{staged ? stage : I.cols, I.llr, I.tam, S.w, S.K, cd.nwp, cd.nw, S.nprefix,
-                   S.base};
+        skip_known = false;
+      }
+      if (!skip_known || s_ml) {
+        skip = tile_skip(J, J.seg[cs], J.it[s_iter], s_ml);
+        skip_known = true;
+      }
+      bool published = false;
+      if (!skip) {
         LaneBest lb;
         lb.reset();
-        if (ml) eval_dispatch<true>(cd.nw, sv, b.ncr, sw, lt - S.tile_lo, lb);
-        else eval_dispatch<false>(cd.nw, sv, b.ncr, sw, lt - S.tile_lo, lb);
-        if (!ml) {
+        const unsigned long long st = lt - cs_lo;
+        if (s_runs) {
+          if (cc < 0 || st < cc_lo || st >= cc_hi) {
+            // run c holding segment tile st: largest c with cum[c] <= st
+            int clo = 0, chi = sv.tam - 2;
+            while (clo < chi) {
+              const int mid = (clo + chi + 1) >> 1;
+              if (s_cum[mid] <= st) clo = mid;
+              else chi = mid - 1;
+            }
+            cc = clo;
+            cc_lo = s_cum[clo];
+            cc_hi = cc_lo + run_tiles(b.ncr, clo, sv.w, kRunKK);
+          }
+          const unsigned long long r0 = (st - cc_lo) * (32ull * kRunKK);
+          if (s_ml) eval_run_dispatch<true, kRunKK>(s_nw, sv, b.ncr, sw, cc, r0, lb);
+          else eval_run_dispatch<false, kRunKK>(s_nw, sv, b.ncr, sw, cc, r0, lb);
+        } else {
+          if (s_ml) eval_dispatch<true>(s_nw, sv, b.ncr, sw, st, lb);
+          else eval_dispatch<false>(s_nw, sv, b.ncr, sw, st, lb);
+        }
+        if (!s_ml) {
           const unsigned long long g = warp_min_u64(lb.g);
-          if (lane == 0 && g != kNone) atomicMin(&J.best, g);
+          if (g != kNone) {
+            published = true;
+            skip_known = false;
+            if (lane == 0) atomicMin(&J.best, g);
+          }
         } else {
           uint32_t o = lb.o;
           unsigned long long r = lb.r;
           warp_min_key(o, r);
-          if (lane == 0 && o != 0xffffffffu)
-            if (!atomic_min_key(J.mlkey[S.iter][S.w], o, r)) atomicOr(b.status, kStatusCasLimit);
+          if (o != 0xffffffffu) {
+            published = true;
+            if (lane == 0 && !atomic_min_key(J.mlkey[s_iter][sv.w], o, r))
+              atomicOr(b.status, kStatusCasLimit);
+          }
         }
       }
-      int last = 0;
-      if (lane == 0) {
-        __threadfence();
-        last = (atomicAdd(&J.tiles_done, 1ull) + 1ull == J.ntiles) ? 1 : 0;
-      }
-      last = __shfl_sync(kFull, last, 0);
-      if (last) {
-        __threadfence();
-        Winner wn;
-        if (!ml)
-          wn = winner_from_index(J, *reinterpret_cast<volatile unsigned long long *>(&J.best),
-                                 cd.variant == kProb);
-        else
-          wn = winner_ml(J);
-        finish_shot(b, cd, J, J.shot, wn, J.ebits, s_delta[warp]);
+      // tiles of this fetch done for the current job: posted once per job per fetch
+      pending += 1ull;
+      fenced = fenced || published;
+      const bool flush = (t + 1 == t1) || (t + 1 >= cj_hi);
+      if (flush) {
+        int last = 0;
+        if (lane == 0) {
+          if (fenced) __threadfence();  // order the published minima before the count
+          last = (atomicAdd(&J.tiles_done, pending) + pending == J.ntiles) ? 1 : 0;
+        }
+        pending = 0;
+        fenced = false;
+        last = __shfl_sync(kFull, last, 0);
+        if (last) {
+          __threadfence();
+          Winner wn;
+          if (!s_ml)
+            wn = winner_from_index(J, *reinterpret_cast<volatile unsigned long long *>(&J.best),
+                                   s_prob != 0);
+          else
+            wn = winner_ml(J);
+          finish_shot(b, *cdp, J, J.shot, wn, J.ebits, s_delta[warp]);
+        }
       }
     }
   }

@@ -31,6 +31,7 @@ _SIGS = {
     "grand_engine_kernel_times": ([VP, VP, ctypes.POINTER(ctypes.c_float),
                                    ctypes.POINTER(ctypes.c_float)], ctypes.c_int),
     "grand_measure_int_peak": ([], ctypes.c_double),
+    "grand_device_info": ([ctypes.c_char_p, ctypes.c_int], ctypes.c_int),
 }
 capi.SIGNATURES.update(_SIGS)
 
@@ -145,6 +146,11 @@ class Engine:
 
     def int_peak(self):
         return self.lib.grand_measure_int_peak()
+
+    def device_info(self) -> str:
+        buf = ctypes.create_string_buffer(256)
+        self.lib.grand_device_info(buf, 256)
+        return buf.value.decode()
 
 
 def offsets_for(rec_lens, shot_code):
