@@ -14,8 +14,8 @@ Reported (one JSON line, rank 0):
              from host buffers, copies included;
   roofline   the search kernel on the stress input the integer roofline is
              defined on (random syndromes, W = 4, exhaustive enumeration), ops
-             counted as (w+1)*ceil(R/32) per candidate, against the measured
-             lop3 issue rate of this GPU;
+             counted as ceil(R/32)+1 per candidate (the fixed (w+1)*ceil(R/32)
+             count is reported beside it), against the measured lop3 issue rate;
   cpu_baseline  the upstream CPU search algorithm (its C restatement in oracle/,
              or the upstream library itself where it was built) on all host cores.
 
@@ -344,18 +344,39 @@ def run_ours(args):
     return out
 
 
-def stress_roofline(torch, lib, dev, sp):
-    """Search kernel on exhaustive random-syndrome shots of [[144,12,12]], W=4."""
+STRESS_SHOTS = 192
+# DRAM bytes (read + write) of one search_kernel launch on the stress input, from an ncu
+# --set full capture of `bench.py --case stress` (48 shots), scaled to 192 shots.
+STRESS_TRAFFIC_PER_SHOT = (1.023488e6 + 21.76e3) / 48
+
+
+def stress_case(torch, lib, dev, n=STRESS_SHOTS):
+    """Engine + device buffers for exhaustive random-syndrome shots of [[144,12,12]], W=4."""
     from library_s_grand_gb300 import capi, synth
     from library_s_grand_gb300.engine import Engine
     code = synth.BB_CODES[144]()
-    n = 192
     syn = (np.random.default_rng(1).random((n, code.n)) < 0.5).astype(np.int32)
-    cands, ops = stress_ops(code.hz, syn, 4)
     eng = Engine(lib)
     eng.add_css(code.hx, code.hz, "x", False, capi.GrandDecoderConfig(4, 256, 0, 300, 10, -1))
     d_rec = torch.from_numpy(syn.ravel()).to(dev)
     d_res = torch.empty(n * 72, dtype=torch.uint8, device=dev)
+    return code, syn, eng, d_rec, d_res
+
+
+def stress_roofline(torch, lib, dev, sp):
+    """Search kernel on exhaustive random-syndrome shots of [[144,12,12]], W=4.
+
+    Convention: a candidate needs ceil(R/32) XOR-OR word operations against the
+    prefix-reduced target plus one minimum, i.e. 4 integer ops for R = 72, once
+    the prefix XOR is hoisted out of the last-index loop; the peak is the lop3
+    issue rate measured on this GPU.  The fixed per-candidate count
+    (w+1)*ceil(R/32), which charges the full XOR of w columns to every candidate,
+    is reported beside it."""
+    from library_s_grand_gb300 import capi
+    n = STRESS_SHOTS
+    code, syn, eng, d_rec, d_res = stress_case(torch, lib, dev, n)
+    cands, ops_fixed = stress_ops(code.hz, syn, 4)
+    words = math.ceil(code.n / 32)
     times = []
     for rep in range(4):
         eng.decode_device(n, d_rec.data_ptr(), d_res.data_ptr(), sp, use_graph=False)
@@ -367,14 +388,51 @@ def stress_roofline(torch, lib, dev, sp):
     assert int(res["total_tested_combinations"].sum()) == cands, "count mismatch"
     search_ms = float(np.median(times[1:]))
     peak = eng.int_peak()
-    achieved = ops / (search_ms * 1e-3)
+    rate = cands / (search_ms * 1e-3)
+    achieved = rate * (words + 1)
     return {"bound": "int_alu", "achieved": achieved / 1e9, "peak": peak / 1e9, "unit": "Gop/s",
-            "frac": achieved / peak, "traffic": None, "kernel": "search_kernel",
+            "frac": achieved / peak, "traffic": STRESS_TRAFFIC_PER_SHOT * n,
+            "traffic_unit": "bytes per launch (ncu, scaled from 48 shots)",
+            "kernel": "search_kernel",
             "workload": f"{n} random-syndrome shots of BB[[144,12,12]], W=4, exhaustive "
                         f"({cands} candidates, 3 threshold iterations)",
-            "ops_per_candidate": "(w+1)*ceil(72/32)", "search_ms": search_ms,
-            "candidates_per_s": cands / (search_ms * 1e-3),
+            "ops_per_candidate": f"ceil(R/32)+1 = {words + 1} (XOR-OR words + min)",
+            "search_ms": search_ms, "candidates_per_s": rate,
+            "frac_fixed_convention": ops_fixed / (search_ms * 1e-3) / peak,
+            "fixed_convention": "(w+1)*ceil(R/32) ops per candidate",
             "peak_source": "lop3.b32 issue rate measured on this GPU (grand_measure_int_peak)"}
+
+
+def run_case(args):
+    """Profiling entry point: run one case a few times, print kernel times only."""
+    import torch
+    from library_s_grand_gb300 import build as B
+    from library_s_grand_gb300 import capi, synth
+    from library_s_grand_gb300.engine import Engine
+    B.build()
+    lib = capi.load_library()
+    dev = torch.device("cuda", 0)
+    sp = torch.cuda.current_stream(dev).cuda_stream
+    if args.case == "stress":
+        code, syn, eng, d_rec, d_res = stress_case(torch, lib, dev, args.case_shots or 48)
+        n = len(syn)
+    else:
+        tmp = tempfile.mkdtemp()
+        phase = synth.write_phase_file(os.path.join(tmp, "phase.txt"), PHASE)
+        code, errors = workload(0)
+        eng = Engine(lib)
+        eng.add_css(code.hx, code.hz, "x", True, capi.GrandDecoderConfig(W_MAX, 256, 0, CAP, 10, -1),
+                    phase)
+        n = SHOTS
+        d_rec = torch.from_numpy(np.ascontiguousarray(errors.ravel())).to(dev)
+        d_res = torch.empty(n * 72, dtype=torch.uint8, device=dev)
+    for _ in range(args.case_reps):
+        if eng.decode_device(n, d_rec.data_ptr(), d_res.data_ptr(), sp, use_graph=False) != 0:
+            raise RuntimeError("decode failed")
+        if eng.sync_status(sp) != 0:
+            raise RuntimeError("status error")
+        tri, sea = eng.kernel_times(sp)
+        print(f"case {args.case}: triage {tri:.4f} ms  search {sea:.4f} ms", flush=True)
 
 
 def run_reference(args):
@@ -416,8 +474,15 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--case", choices=["stress", "headline"], default=None,
+                    help="profiling mode: run one case --case-reps times, print kernel times")
+    ap.add_argument("--case-reps", type=int, default=2)
+    ap.add_argument("--case-shots", type=int, default=0)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.case:
+        run_case(args)
+        return
     out = run_reference(args) if args.impl == "reference" else run_ours(args)
     if out is not None:
         print(json.dumps(out), flush=True)

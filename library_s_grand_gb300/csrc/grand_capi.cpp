@@ -9,6 +9,10 @@
 #include <string.h>
 
 #include <vector>
+#include <mutex>
+#include <string>
+
+#include <sys/stat.h>
 
 #include "grand_host.h"
 
@@ -41,6 +45,26 @@ Masks read_masks(const char *path) {
     ++mk.n;
   }
   fclose(f);
+  return mk;
+}
+
+// The same, remembered per (path, modification time, size): callers decode batch
+// after batch with the same mask file.
+Masks read_masks_cached(const char *path) {
+  static std::mutex mu;
+  static std::string last_path;
+  static long long last_mtime = -1, last_size = -1;
+  static Masks last;
+  struct stat st;
+  if (!path || stat(path, &st) != 0) return read_masks(path);
+  const long long mt = (long long)st.st_mtim.tv_sec * 1000000000LL + st.st_mtim.tv_nsec;
+  std::lock_guard<std::mutex> lk(mu);
+  if (last_path == path && last_mtime == mt && last_size == (long long)st.st_size) return last;
+  Masks mk = read_masks(path);
+  last_path = path;
+  last_mtime = mt;
+  last_size = (long long)st.st_size;
+  last = mk;
   return mk;
 }
 
@@ -79,7 +103,7 @@ bool read_llr_file(const char *path, std::vector<float> &llr, int m) { return re
 
 // Phase masks for a registered code: the upstream checks, in upstream order.
 int read_masks_into(const char *path, CallParams *p, int W) {
-  Masks mk = read_masks(path);
+  Masks mk = read_masks_cached(path);
   p->num_phases = num_phases_for(W);
   if (p->num_phases == 0) {
     fprintf(stderr, "Invalid max_error_weight: %d. Must be 6 or 7.\n", W);
@@ -189,7 +213,7 @@ int decode_css(int variant, const int *Hx, const int *Hz, int n, int m, const in
   CallParams p;
   p.variant = variant;
   if (variant == kProb) {
-    mk = read_masks(pfile);
+    mk = read_masks_cached(pfile);
     p.num_phases = num_phases_for(W);
     if (p.num_phases == 0) {
       fprintf(stderr, "Invalid max_error_weight: %d. Must be 6 or 7.\n", W);
@@ -261,7 +285,7 @@ int decode_dem(int variant, const int *H, const int *L, int n, int m, int nl, co
   CallParams p;
   p.variant = variant;
   if (variant == kProb) {
-    Masks mk = read_masks(file);
+    Masks mk = read_masks_cached(file);
     if (mk.n == 0) {
       fprintf(stderr, "No phase order masks read from: %s\n", file ? file : "(null)");
       return GRAND_ERR_INVALID;

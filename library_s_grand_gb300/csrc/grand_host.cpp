@@ -38,6 +38,7 @@ Tuning &tuning() {
     if (const char *s = getenv("GRAND_LIGHT_LOG2")) x.light_max_log2 = std::max(0, std::min(40, atoi(s)));
     if (const char *s = getenv("GRAND_TILE_K")) x.tile_k = std::max(1, std::min(64, atoi(s)));
     if (const char *s = getenv("GRAND_SEARCH_GRID_MULT")) x.search_grid_mult = std::max(0, atoi(s));
+    if (const char *s = getenv("GRAND_ZERO_COPY")) x.zero_copy = atoi(s) != 0;
     return x;
   }();
   return t;
@@ -68,6 +69,7 @@ Workspace::~Workspace() {
   void *bufs[] = {d_in, d_in2, d_res, d_dec, d_declog, d_cost, d_jobs, d_scratch, d_small,
                   d_deferred, d_map, d_codes, d_llr, d_off, d_shotcode};
   for (void *b : bufs) cudaFree(b);
+  if (h_codes) cudaFreeHost(h_codes);
   for (auto &e : ev) if (e) cudaEventDestroy(e);
   if (stream) cudaStreamDestroy(stream);
 }
@@ -202,26 +204,36 @@ static cudaError_t upload(T **d, const std::vector<T> &h) {
 
 std::shared_ptr<CodeTables> Context::tables(int family, const int *H, const int *H_other,
                                             const int *L, int n, int m, int nl, int *err) {
-  std::vector<int> key;
   const size_t nm = (size_t)n * m;
-  key.reserve(6 + nm * (family == kCss ? 2 : 1) + (size_t)m * nl);
+  const int *second = family == kCss ? H_other : L;
+  const size_t second_len = family == kCss ? nm : (size_t)m * nl;
+  // Cache hit test: exact content comparison against the caller's arrays (no copy).
+  auto same = [&](const CodeTables &c) {
+    if (c.family != family || c.R != n || c.m != m || c.n_logicos != nl) return false;
+    if (c.key.size() != 4 + nm + second_len) return false;
+    if (memcmp(c.key.data() + 4, H, nm * sizeof(int)) != 0) return false;
+    return second_len == 0 || memcmp(c.key.data() + 4 + nm, second, second_len * sizeof(int)) == 0;
+  };
+  {
+    std::lock_guard<std::mutex> lk(mu_);
+    for (size_t i = cache_.size(); i-- > 0;)
+      if (same(*cache_[i])) {
+        auto t = cache_[i];
+        if (i + 1 != cache_.size()) {
+          cache_.erase(cache_.begin() + i);
+          cache_.push_back(t);
+        }
+        return t;
+      }
+  }
+  std::vector<int> key;
+  key.reserve(4 + nm + second_len);
   key.push_back(family);
   key.push_back(n);
   key.push_back(m);
   key.push_back(nl);
   key.insert(key.end(), H, H + nm);
-  if (family == kCss) key.insert(key.end(), H_other, H_other + nm);
-  else if (nl > 0) key.insert(key.end(), L, L + (size_t)m * nl);
-  {
-    std::lock_guard<std::mutex> lk(mu_);
-    for (size_t i = 0; i < cache_.size(); ++i)
-      if (cache_[i]->key == key) {
-        auto t = cache_[i];
-        cache_.erase(cache_.begin() + i);
-        cache_.push_back(t);
-        return t;
-      }
-  }
+  if (second_len) key.insert(key.end(), second, second + second_len);
   auto t = std::make_shared<CodeTables>();
   t->family = family;
   t->R = n;
@@ -342,15 +354,20 @@ int run_batch(Context *ctx, Workspace *ws, const BatchRequest &req, BatchTiming 
   const Tuning &tn = tnp ? *tnp : tuning();
   const int ncodes = (int)req.codes.size();
 
+  // Zero-copy: the GPU reads the caller's records and writes its results in
+  // place, over NVLink-C2C, when the device can access pageable host memory.
+  const bool zc = tn.zero_copy && ctx->pageable_access;
   CK(ensure(&ws->d_codes, &ws->cap_codes, sizeof(DevCode) * ncodes));
-  CK(ensure(&ws->d_in, &ws->cap_in, req.in_ints * sizeof(int)));
-  if (req.h_in_log) CK(ensure(&ws->d_in2, &ws->cap_in2, req.in_log_ints * sizeof(int)));
-  if (req.h_off) CK(ensure(&ws->d_off, &ws->cap_off, sizeof(long long) * N));
-  if (req.h_shot_code) CK(ensure(&ws->d_shotcode, &ws->cap_shotcode, sizeof(int) * N));
-  CK(ensure(&ws->d_res, &ws->cap_res, sizeof(GrandDecoderResult) * N));
-  if (req.h_dec_err) CK(ensure(&ws->d_dec, &ws->cap_dec, (size_t)N * req.dec_m));
-  if (req.h_dec_log) CK(ensure(&ws->d_declog, &ws->cap_declog, (size_t)N * std::max(req.dec_nl, 1)));
-  if (req.h_cost) CK(ensure(&ws->d_cost, &ws->cap_cost, sizeof(float) * N));
+  if (!zc) {
+    CK(ensure(&ws->d_in, &ws->cap_in, req.in_ints * sizeof(int)));
+    if (req.h_in_log) CK(ensure(&ws->d_in2, &ws->cap_in2, req.in_log_ints * sizeof(int)));
+    if (req.h_off) CK(ensure(&ws->d_off, &ws->cap_off, sizeof(long long) * N));
+    if (req.h_shot_code) CK(ensure(&ws->d_shotcode, &ws->cap_shotcode, sizeof(int) * N));
+    CK(ensure(&ws->d_res, &ws->cap_res, sizeof(GrandDecoderResult) * N));
+    if (req.h_dec_err) CK(ensure(&ws->d_dec, &ws->cap_dec, (size_t)N * req.dec_m));
+    if (req.h_dec_log) CK(ensure(&ws->d_declog, &ws->cap_declog, (size_t)N * std::max(req.dec_nl, 1)));
+    if (req.h_cost) CK(ensure(&ws->d_cost, &ws->cap_cost, sizeof(float) * N));
+  }
   const int max_jobs = std::min(N, 16384);
   CK(ensure(&ws->d_jobs, &ws->cap_jobs, sizeof(Job) * max_jobs));
   const size_t scratch_words = 32ull << 20;
@@ -359,31 +376,55 @@ int run_batch(Context *ctx, Workspace *ws, const BatchRequest &req, BatchTiming 
   CK(ensure(&ws->d_small, &small_cap, 256));
   CK(ensure(&ws->d_deferred, &ws->cap_deferred, sizeof(int) * N));
 
+  const size_t code_bytes = sizeof(DevCode) * ncodes;
+  if (ws->cap_hcodes < code_bytes) {
+    // the previous copy from this buffer may still be in flight on this stream
+    CK(cudaStreamSynchronize(s));
+    if (ws->h_codes) cudaFreeHost(ws->h_codes);
+    ws->h_codes = nullptr;
+    ws->cap_hcodes = 0;
+    CK(cudaHostAlloc(&ws->h_codes, std::max<size_t>(code_bytes, 4096), cudaHostAllocDefault));
+    ws->cap_hcodes = std::max<size_t>(code_bytes, 4096);
+  }
+  memcpy(ws->h_codes, req.codes.data(), code_bytes);  // stream is idle between calls
   CK(cudaEventRecord(ws->ev[0], s));
-  CK(cudaMemcpyAsync(ws->d_codes, req.codes.data(), sizeof(DevCode) * ncodes,
-                     cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync(ws->d_in, req.h_in, req.in_ints * sizeof(int), cudaMemcpyHostToDevice, s));
-  if (req.h_in_log)
-    CK(cudaMemcpyAsync(ws->d_in2, req.h_in_log, req.in_log_ints * sizeof(int),
-                       cudaMemcpyHostToDevice, s));
-  if (req.h_off)
-    CK(cudaMemcpyAsync(ws->d_off, req.h_off, sizeof(long long) * N, cudaMemcpyHostToDevice, s));
-  if (req.h_shot_code)
-    CK(cudaMemcpyAsync(ws->d_shotcode, req.h_shot_code, sizeof(int) * N, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(ws->d_codes, ws->h_codes, code_bytes, cudaMemcpyHostToDevice, s));
+  if (!zc) {
+    CK(cudaMemcpyAsync(ws->d_in, req.h_in, req.in_ints * sizeof(int), cudaMemcpyHostToDevice, s));
+    if (req.h_in_log)
+      CK(cudaMemcpyAsync(ws->d_in2, req.h_in_log, req.in_log_ints * sizeof(int),
+                         cudaMemcpyHostToDevice, s));
+    if (req.h_off)
+      CK(cudaMemcpyAsync(ws->d_off, req.h_off, sizeof(long long) * N, cudaMemcpyHostToDevice, s));
+    if (req.h_shot_code)
+      CK(cudaMemcpyAsync(ws->d_shotcode, req.h_shot_code, sizeof(int) * N,
+                         cudaMemcpyHostToDevice, s));
+  }
   CK(cudaEventRecord(ws->ev[1], s));
 
   DevBatch b;
   memset(&b, 0, sizeof(b));
   b.num_codes = ncodes;
   b.codes = (const DevCode *)ws->d_codes;
-  b.in = (const int *)ws->d_in;
-  b.in_off = req.h_off ? (const long long *)ws->d_off : nullptr;
-  b.in_log = req.h_in_log ? (const int *)ws->d_in2 : nullptr;
-  b.shot_code = req.h_shot_code ? (const int *)ws->d_shotcode : nullptr;
-  b.results = (GrandDecoderResult *)ws->d_res;
-  b.dec_err = req.h_dec_err ? (unsigned char *)ws->d_dec : nullptr;
-  b.dec_log = req.h_dec_log ? (unsigned char *)ws->d_declog : nullptr;
-  b.ml_cost = req.h_cost ? (float *)ws->d_cost : nullptr;
+  if (zc) {
+    b.in = req.h_in;
+    b.in_off = req.h_off;
+    b.in_log = req.h_in_log;
+    b.shot_code = req.h_shot_code;
+    b.results = req.h_results;
+    b.dec_err = req.h_dec_err;
+    b.dec_log = req.h_dec_log;
+    b.ml_cost = req.h_cost;
+  } else {
+    b.in = (const int *)ws->d_in;
+    b.in_off = req.h_off ? (const long long *)ws->d_off : nullptr;
+    b.in_log = req.h_in_log ? (const int *)ws->d_in2 : nullptr;
+    b.shot_code = req.h_shot_code ? (const int *)ws->d_shotcode : nullptr;
+    b.results = (GrandDecoderResult *)ws->d_res;
+    b.dec_err = req.h_dec_err ? (unsigned char *)ws->d_dec : nullptr;
+    b.dec_log = req.h_dec_log ? (unsigned char *)ws->d_declog : nullptr;
+    b.ml_cost = req.h_cost ? (float *)ws->d_cost : nullptr;
+  }
   b.ncr = ctx->d_ncr;
   b.jobs = (Job *)ws->d_jobs;
   b.max_jobs = max_jobs;
@@ -434,15 +475,17 @@ int run_batch(Context *ctx, Workspace *ws, const BatchRequest &req, BatchTiming 
   }
 
   CK(cudaEventRecord(ws->ev[4], s));
-  CK(cudaMemcpyAsync(req.h_results, ws->d_res, sizeof(GrandDecoderResult) * N,
-                     cudaMemcpyDeviceToHost, s));
-  if (req.h_dec_err)
-    CK(cudaMemcpyAsync(req.h_dec_err, ws->d_dec, (size_t)N * req.dec_m, cudaMemcpyDeviceToHost, s));
-  if (req.h_dec_log && req.dec_nl > 0)
-    CK(cudaMemcpyAsync(req.h_dec_log, ws->d_declog, (size_t)N * req.dec_nl,
+  if (!zc) {
+    CK(cudaMemcpyAsync(req.h_results, ws->d_res, sizeof(GrandDecoderResult) * N,
                        cudaMemcpyDeviceToHost, s));
-  if (req.h_cost)
-    CK(cudaMemcpyAsync(req.h_cost, ws->d_cost, sizeof(float) * N, cudaMemcpyDeviceToHost, s));
+    if (req.h_dec_err)
+      CK(cudaMemcpyAsync(req.h_dec_err, ws->d_dec, (size_t)N * req.dec_m, cudaMemcpyDeviceToHost, s));
+    if (req.h_dec_log && req.dec_nl > 0)
+      CK(cudaMemcpyAsync(req.h_dec_log, ws->d_declog, (size_t)N * req.dec_nl,
+                         cudaMemcpyDeviceToHost, s));
+    if (req.h_cost)
+      CK(cudaMemcpyAsync(req.h_cost, ws->d_cost, sizeof(float) * N, cudaMemcpyDeviceToHost, s));
+  }
   CK(cudaEventRecord(ws->ev[5], s));
   CK(cudaStreamSynchronize(s));
   float h2d = 0, d2h = 0;

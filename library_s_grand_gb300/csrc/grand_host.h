@@ -67,6 +67,7 @@ struct Workspace {
   void *d_deferred = nullptr; size_t cap_deferred = 0;
   void *d_map = nullptr; size_t cap_map = 0;
   void *d_codes = nullptr; size_t cap_codes = 0;
+  void *h_codes = nullptr; size_t cap_hcodes = 0;  // pinned staging of the DevCode array
   void *d_llr = nullptr; size_t cap_llr = 0;
   void *d_off = nullptr; size_t cap_off = 0;
   void *d_shotcode = nullptr; size_t cap_shotcode = 0;
@@ -123,6 +124,8 @@ struct Tuning {
   int light_max_log2 = 12;
   int tile_k = 4;
   int search_grid_mult = 0;  // CTAs per SM of the search kernel; 0: occupancy maximum
+  int zero_copy = 1;         // read records / write results in the caller's host memory
+                             // when the device can access pageable memory (GRAND_ZERO_COPY)
 };
 Tuning &tuning();  // process defaults (GRAND_LIGHT_LOG2, GRAND_TILE_K, GRAND_SEARCH_GRID_MULT)
 

@@ -126,3 +126,48 @@ def test_tuning_does_not_change_results(gpulib, mix, tile_k, light):
     rc2, got = eng.decode(recs, sc)
     assert rc == rc2 == 0
     assert len(O.fields_equal(got, ref)) == 0
+
+
+def test_zero_copy_and_copy_paths_agree(gpulib, tmp_path):
+    """The C ABI reads records / writes results in host memory directly when the
+    GPU can access pageable memory; GRAND_ZERO_COPY=0 forces staged copies.
+    Both must give identical results, decoded patterns and ML costs."""
+    import os
+    import subprocess
+    import sys
+    from conftest import ROOT, load_golden, write_aux
+    script = tmp_path / "run.py"
+    script.write_text(
+        "import sys, numpy as np\n"
+        f"sys.path.insert(0, {ROOT!r}); sys.path.insert(0, {os.path.join(ROOT, 'tests')!r})\n"
+        "from conftest import load_golden\n"
+        "from library_s_grand_gb300 import capi\n"
+        "lib = capi.load_library()\n"
+        "out = {}\n"
+        "for name, aux in [('cc_bb72_x_err_w3', None), ('ml_dem60_w3_cap20', sys.argv[2])]:\n"
+        "    g = load_golden(name)\n"
+        "    cfg = capi.GrandDecoderConfig(*[int(v) for v in g['cfg']])\n"
+        "    if str(g['kind']) == 'css':\n"
+        "        rc, res, dec = capi.decode_css_ex(lib, 'uniform', g['hx'], g['hz'], g['errors'], None, cfg, 'x')\n"
+        "        cost = np.zeros(1, np.float32)\n"
+        "    else:\n"
+        "        rc, res, dec, dlog, cost = capi.decode_dem_ex(lib, 'ml', g['h'], g['l'], g['detectors'], g['logicals'], cfg, aux)\n"
+        "    assert rc == 0\n"
+        "    out[name + '_res'] = res; out[name + '_dec'] = dec; out[name + '_cost'] = cost\n"
+        "np.savez(sys.argv[1], **out)\n")
+    g = load_golden("ml_dem60_w3_cap20")
+    aux = write_aux(tmp_path, g)
+    outs = []
+    for zc in ("1", "0"):
+        path = tmp_path / f"out{zc}.npz"
+        env = dict(os.environ, GRAND_ZERO_COPY=zc)
+        subprocess.check_call([sys.executable, str(script), str(path), aux], env=env)
+        outs.append(np.load(path))
+    for k in outs[0].files:
+        a, b = outs[0][k], outs[1][k]
+        if a.dtype.names:
+            for f in ("found", "found_weight", "tam", "total_tested_combinations", "iteration",
+                      "degenerate", "is_equal", "hibrido"):
+                assert np.array_equal(a[f], b[f]), (k, f)
+        else:
+            assert np.array_equal(a, b), k
