@@ -152,6 +152,28 @@ int grand_decode_ML_cln_ex(int *H_dem, const int *L_dem, int n, int m, int n_log
                            const GrandDecoderConfig *config, GrandDecoderResult *results,
                            const char *llr_file, const GrandDecodeOutputs *out);
 
+/* No counterpart in the upstream library.  grand_decode_cc with syndrome input
+ * for callers that may not allocate device memory while running (a real-time
+ * decoding loop that reserved its memory at start-up, a process whose device
+ * memory belongs to another framework's pool): it calls no cudaMalloc, cudaFree
+ * or other allocating routine.  d_H (n x m int32, the matrix that decodes the
+ * syndromes, i.e. Hz for X errors), d_syndromes (num_shots x n int32) and
+ * d_results (num_shots records) are device pointers owned by the caller; results
+ * equal grand_decode_cc(Hx, Hz, n, m, NULL, syndromes, ...) field for field, with
+ * zero timing fields.  Everything else lives in one fixed file-scope device array
+ * of about 25 MiB, held by every GPU that loads it until the process exits.
+ * Limits: n <= 256, m <= 1024 (larger sizes return GRAND_ERR_LIMIT with a
+ * message); hard shots share a 16 MiB search arena per 2048-shot chunk and an
+ * exhausted arena also returns GRAND_ERR_LIMIT.  The first call on a device does
+ * its set-up (looks up the array's device address, fills its binomial table) and
+ * synchronizes `stream`: make it before any stream capture.  Every call reuses
+ * the same array, so calls that overlap on the GPU (other threads, other
+ * streams) race; the call itself returns only when its work on `stream`
+ * (a cudaStream_t, NULL for the legacy default stream) has finished. */
+int grand_decode_cc_noalloc(const int *d_H, int n, int m, const int *d_syndromes, int num_shots,
+                            const GrandDecoderConfig *config, GrandDecoderResult *d_results,
+                            void *stream);
+
 /* Library version string and last error message of the calling thread. */
 const char *grand_version(void);
 const char *grand_last_error(void);

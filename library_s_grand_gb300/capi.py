@@ -88,6 +88,9 @@ SIGNATURES = {
     "grand_decode_cln_ex": (_DEM + [_OUT], ctypes.c_int),
     "grand_decode_prob_cln_ex": (_DEM + [ctypes.c_char_p, _OUT], ctypes.c_int),
     "grand_decode_ML_cln_ex": (_DEM + [ctypes.c_char_p, _OUT], ctypes.c_int),
+    "grand_decode_cc_noalloc": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                 ctypes.c_int, ctypes.POINTER(GrandDecoderConfig),
+                                 ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "grand_version": ([], ctypes.c_char_p),
     "grand_last_error": ([], ctypes.c_char_p),
 }

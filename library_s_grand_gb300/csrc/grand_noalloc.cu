@@ -1,0 +1,263 @@
+// grand_noalloc.cu -- grand_decode_cc_noalloc: a decode that allocates nothing.
+//
+// Who needs it: callers that must not allocate device memory once they are
+// running -- a real-time decoding loop in a quantum-control stack that reserves
+// its memory up front and may not stall in the allocator mid-experiment, or a
+// host process whose device memory is already entirely owned by another
+// framework's pool.  The regular entry points allocate their workspaces with
+// cudaMalloc on first use (and grow them); this one keeps everything it needs
+// beyond the caller's inputs and outputs in one fixed, file-scope device array.
+//
+// The batch runs through the same triage and search kernels as the other entry
+// points.  Only the place their scratch lives differs: the binomial table, the
+// packed columns, the code descriptor, the counters, the job table and the
+// scratch arena are carved out of g_noalloc_scratch.
+#include <cuda_runtime.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <mutex>
+
+#include "grand_common.h"
+#include "grand_host.h"
+
+namespace grand {
+namespace {
+
+// Limits of the no-allocation path.
+constexpr int kNaMaxRows = 256;                     // R <= 256 (8 words per column)
+constexpr int kNaMaxCols = 1024;                    // m <= 1024
+constexpr int kNaChunk = 2048;                      // shots per launch = job slots
+constexpr unsigned long long kNaArenaWords = 4ull << 20;  // 16 MiB of staged search data
+
+constexpr size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+constexpr size_t kOffNcr = 0;
+constexpr size_t kOffCode = align256(kOffNcr + sizeof(unsigned long long) * (kMaxTam + 1) * (kMaxW + 1));
+constexpr size_t kOffCols = align256(kOffCode + sizeof(DevCode));
+constexpr size_t kOffColw = align256(kOffCols + sizeof(uint32_t) * kNaMaxCols * 8);
+constexpr size_t kOffSmall = align256(kOffColw + sizeof(int) * kNaMaxCols);  // counters, +128: status
+constexpr size_t kOffDeferred = align256(kOffSmall + 256);
+constexpr size_t kOffJobs = align256(kOffDeferred + sizeof(int) * kNaChunk);
+constexpr size_t kOffArena = align256(kOffJobs + sizeof(Job) * kNaChunk);
+constexpr size_t kScratchBytes = align256(kOffArena + sizeof(uint32_t) * kNaArenaWords);
+
+}  // namespace
+
+// All no-allocation calls on a device share this array; it exists for the life
+// of the process on every device that loads this part of the library.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
+
+namespace {
+
+// C(n, k) by the same multiplicative formula as the host table.
+__global__ void noalloc_ncr_kernel(unsigned long long *t) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n > kMaxTam) return;
+  for (int k = 0; k <= kMaxW; ++k) {
+    unsigned long long r = 0;
+    if (k <= n) {
+      r = 1;
+      if (k != 0 && k != n)
+        for (int i = 1; i <= k; ++i) r = r * (unsigned long long)(n - i + 1) / (unsigned long long)i;
+    }
+    t[n * (kMaxW + 1) + k] = r;
+  }
+}
+
+// One thread per column: packed bits (LSB-first, nwp words) and the column weight.
+__global__ void noalloc_pack_kernel(const int *H, int n, int m, int nwp, uint32_t *cols, int *colw) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m) return;
+  uint32_t w[8] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
+  int sum = 0;
+  for (int r = 0; r < n; ++r) {
+    const int v = H[(size_t)r * m + c];
+    sum += v;
+    if (v != 0) w[r >> 5] |= 1u << (r & 31);
+  }
+  for (int i = 0; i < nwp; ++i) cols[(size_t)c * nwp + i] = w[i];
+  colw[c] = sum;
+}
+
+// One block: maximum column weight and regularity, then the code descriptor.
+__global__ void noalloc_code_kernel(DevCode tmpl, const int *colw, int m, DevCode *out) {
+  __shared__ int s_max, s_irregular;
+  if (threadIdx.x == 0) {
+    s_max = 0;
+    s_irregular = 0;
+  }
+  __syncthreads();
+  int mx = 0, irr = 0;
+  const int c0 = colw[0];
+  for (int c = threadIdx.x; c < m; c += blockDim.x) {
+    mx = max(mx, colw[c]);
+    irr |= colw[c] != c0;
+  }
+  atomicMax(&s_max, mx);
+  if (irr) atomicOr(&s_irregular, 1);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    tmpl.max_soma = s_max;
+    tmpl.regular = s_irregular ? 0 : 1;
+    *out = tmpl;
+  }
+}
+
+std::mutex g_mu;
+unsigned char *g_base[64] = {};  // device address of g_noalloc_scratch per device
+int g_sms[64] = {}, g_tbps[64] = {}, g_sbps[64] = {};
+
+}  // namespace
+}  // namespace grand
+
+using namespace grand;
+
+extern "C" int grand_decode_cc_noalloc(const int *d_H, int n, int m, const int *d_syndromes,
+                                       int num_shots, const GrandDecoderConfig *config,
+                                       GrandDecoderResult *d_results, void *stream) {
+  if (!config) {
+    fprintf(stderr, "grand: config is NULL\n");
+    return GRAND_ERR_INVALID;
+  }
+  const int W = config->max_error_weight;
+  if (W <= 0 || W > 7) {
+    fprintf(stderr, "Invalid max_error_weight: %d. Must be between 1 and 7.\n", W);
+    return GRAND_ERR_INVALID;
+  }
+  if (num_shots < 0) {
+    fprintf(stderr, "grand_decode_cc_noalloc: negative shot count\n");
+    return GRAND_ERR_INVALID;
+  }
+  if (num_shots == 0) return 0;
+  if (!d_H || !d_syndromes || !d_results) {
+    fprintf(stderr, "grand_decode_cc_noalloc: NULL matrix, syndrome or result pointer\n");
+    return GRAND_ERR_INVALID;
+  }
+  if (n <= 0 || n > kNaMaxRows || m <= 0 || m > kNaMaxCols) {
+    fprintf(stderr,
+            "grand_decode_cc_noalloc: H is %d x %d; this entry point supports at most %d rows and "
+            "%d columns (its scratch is a fixed %zu-byte device array)\n",
+            n, m, kNaMaxRows, kNaMaxCols, (size_t)kScratchBytes);
+    return GRAND_ERR_LIMIT;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess || dev < 0 || dev >= 64) {
+    fprintf(stderr, "grand_decode_cc_noalloc: no usable CUDA device (%s)\n", cudaGetErrorString(e));
+    return GRAND_ERR_CUDA;
+  }
+  unsigned char *base = nullptr;
+  {
+    // Set-up, once per device, with that device current: the device address of
+    // the scratch array and its binomial table.
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (!g_base[dev]) {
+      void *ptr = nullptr;
+      e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+      if (e != cudaSuccess) {
+        fprintf(stderr, "grand_decode_cc_noalloc: cudaGetSymbolAddress failed (%s)\n",
+                cudaGetErrorString(e));
+        return GRAND_ERR_CUDA;
+      }
+      int sms = 0, tb = 0, sb = 0;
+      e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      if (e == cudaSuccess) e = occupancy(&tb, &sb);
+      if (e == cudaSuccess) {
+        noalloc_ncr_kernel<<<(kMaxTam + 256) / 256, 256, 0, s>>>(
+            reinterpret_cast<unsigned long long *>((unsigned char *)ptr + kOffNcr));
+        e = cudaGetLastError();
+      }
+      if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+      if (e != cudaSuccess) {
+        fprintf(stderr, "grand_decode_cc_noalloc: set-up failed (%s)\n", cudaGetErrorString(e));
+        return GRAND_ERR_CUDA;
+      }
+      g_sms[dev] = sms;
+      g_tbps[dev] = tb > 0 ? tb : 1;
+      g_sbps[dev] = sb > 0 ? sb : 1;
+      g_base[dev] = (unsigned char *)ptr;
+    }
+    base = g_base[dev];
+  }
+
+  const int nw = (n + 31) / 32;
+  const int nwp = nw <= 2 ? nw : (nw <= 4 ? 4 : 8);
+  uint32_t *cols = reinterpret_cast<uint32_t *>(base + kOffCols);
+  int *colw = reinterpret_cast<int *>(base + kOffColw);
+  DevCode *code = reinterpret_cast<DevCode *>(base + kOffCode);
+
+  DevCode t;
+  memset(&t, 0, sizeof(t));
+  t.R = n;
+  t.m = m;
+  t.nw = nw;
+  t.nwp = nwp;
+  t.mw = (m + 31) / 32;
+  t.family = kCss;
+  t.variant = kUniform;
+  t.input_kind = kInSyndromes;
+  t.W = W;
+  t.Wc = W < kMaxW ? W : kMaxW;
+  t.mode = config->mode_of_search;
+  t.thr = config->threshold_for_hybrid;
+  t.cap = config->max_size_active_positions;
+  t.rec_len = n;
+  t.cols = cols;
+  t.colw = colw;
+
+  noalloc_pack_kernel<<<(m + 127) / 128, 128, 0, s>>>(d_H, n, m, nwp, cols, colw);
+  noalloc_code_kernel<<<1, 256, 0, s>>>(t, colw, m, code);
+  e = cudaGetLastError();
+  // the status word starts at zero for every call; it then collects all chunks
+  if (e == cudaSuccess) e = cudaMemsetAsync(base + kOffSmall + 128, 0, 128, s);
+
+  const Tuning &tn = tuning();
+  for (int lo = 0; lo < num_shots && e == cudaSuccess; lo += kNaChunk) {
+    const int cnt = num_shots - lo < kNaChunk ? num_shots - lo : kNaChunk;
+    DevBatch b;
+    memset(&b, 0, sizeof(b));
+    b.num_shots = cnt;
+    b.num_codes = 1;
+    b.codes = code;
+    b.in = d_syndromes + (size_t)lo * n;
+    b.results = d_results + lo;
+    b.ncr = reinterpret_cast<const unsigned long long *>(base + kOffNcr);
+    b.jobs = reinterpret_cast<Job *>(base + kOffJobs);
+    b.max_jobs = kNaChunk;
+    b.counters = reinterpret_cast<unsigned long long *>(base + kOffSmall);
+    b.status = reinterpret_cast<unsigned *>(base + kOffSmall + 128);
+    b.scratch = reinterpret_cast<uint32_t *>(base + kOffArena);
+    b.scratch_words = kNaArenaWords;
+    b.deferred = reinterpret_cast<int *>(base + kOffDeferred);
+    b.light_max_log2 = tn.light_max_log2;
+    b.tile_k = tn.tile_k;
+    // job and tile counters restart for every chunk
+    e = cudaMemsetAsync(base + kOffSmall, 0, 128, s);
+    const int tgrid_max = g_sms[dev] * g_tbps[dev];
+    const int tgrid = (cnt + 3) / 4 < tgrid_max ? (cnt + 3) / 4 : tgrid_max;
+    if (e == cudaSuccess) e = launch_triage(b, tgrid > 0 ? tgrid : 1, s);
+    if (e == cudaSuccess) e = launch_search(b, g_sms[dev] * g_sbps[dev], s);
+  }
+  unsigned st = 0;
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(&st, base + kOffSmall + 128, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) {
+    fprintf(stderr, "grand_decode_cc_noalloc: CUDA error %s\n", cudaGetErrorString(e));
+    return GRAND_ERR_CUDA;
+  }
+  if (st & (kStatusScratchOverflow | kStatusJobOverflow)) {
+    fprintf(stderr,
+            "grand_decode_cc_noalloc: the fixed %llu-word search arena filled up; "
+            "results of the affected shots are missing -- decode fewer hard shots per call\n",
+            kNaArenaWords);
+    return GRAND_ERR_LIMIT;
+  }
+  if (st & kStatusTamLimit) {
+    fprintf(stderr, "grand_decode_cc_noalloc: an active-position set exceeded %d\n", kMaxTam);
+    return GRAND_ERR_LIMIT;
+  }
+  if (st & kStatusCasLimit) return GRAND_ERR_CUDA;
+  return 0;
+}
