@@ -10,6 +10,7 @@
 #include <tuple>
 #include <vector>
 
+#include "grand_engine_internal.h"
 #include "grand_host.h"
 
 namespace grand {
@@ -19,70 +20,6 @@ bool read_llr_file(const char *path, std::vector<float> &llr, int m);
 }  // namespace grand
 
 using namespace grand;
-
-namespace {
-
-// Job table, scratch and counters of one in-flight device decode.
-struct Slot {
-  void *d_jobs = nullptr; size_t cap_jobs = 0;
-  void *d_scratch = nullptr; size_t cap_scratch = 0;
-  void *d_small = nullptr; size_t cap_small = 0;
-  void *d_deferred = nullptr; size_t cap_deferred = 0;
-  cudaEvent_t ev[3] = {};
-  bool timed = false;
-  ~Slot() {
-    for (auto &e : ev) if (e) cudaEventDestroy(e);
-    cudaFree(d_jobs);
-    cudaFree(d_scratch);
-    cudaFree(d_small);
-    cudaFree(d_deferred);
-  }
-};
-
-struct GraphKey {
-  int n;
-  const void *a, *b, *c, *d;
-  bool operator<(const GraphKey &o) const {
-    return std::tie(n, a, b, c, d) < std::tie(o.n, o.a, o.b, o.c, o.d);
-  }
-};
-
-}  // namespace
-
-struct GrandEngine {
-  Context *ctx = nullptr;
-  std::mutex mu;
-  std::vector<DevCode> codes;
-  std::vector<std::shared_ptr<CodeTables>> tabs;
-  std::vector<float *> llr;
-  std::vector<int> rec_len;
-  void *d_codes = nullptr;
-  size_t cap_codes = 0;
-  bool dirty = true;
-  Tuning tn;
-  std::map<const void *, Slot *> slots;  // per stream
-  std::map<GraphKey, cudaGraphExec_t> graphs;
-  ~GrandEngine() {
-    for (auto &g : graphs) cudaGraphExecDestroy(g.second);
-    for (auto &s : slots) delete s.second;
-    for (float *p : llr) cudaFree(p);
-    cudaFree(d_codes);
-  }
-};
-
-static int upload_codes(GrandEngine *e) {
-  if (!e->dirty) return 0;
-  cudaError_t r = ensure(&e->d_codes, &e->cap_codes, sizeof(DevCode) * std::max<size_t>(1, e->codes.size()));
-  if (r == cudaSuccess && !e->codes.empty())
-    r = cudaMemcpy(e->d_codes, e->codes.data(), sizeof(DevCode) * e->codes.size(),
-                   cudaMemcpyHostToDevice);
-  if (r != cudaSuccess) {
-    set_error("grand: code table upload failed (%s)", cudaGetErrorString(r));
-    return GRAND_ERR_CUDA;
-  }
-  e->dirty = false;
-  return 0;
-}
 
 extern "C" {
 
@@ -271,9 +208,9 @@ int grand_engine_decode_device(GrandEngine *e, int num_shots, const int *d_shot_
   int rc = upload_codes(e);
   if (rc) return rc;
   cudaStream_t s = (cudaStream_t)stream;
-  Slot *&slot = e->slots[stream];
+  EngineSlot *&slot = e->slots[stream];
   if (!slot) {
-    slot = new Slot();
+    slot = new EngineSlot();
     for (auto &ev : slot->ev) cudaEventCreate(&ev);
   }
   const int max_jobs = num_shots;
