@@ -320,6 +320,11 @@ def run_ours(args):
                               res_c["total_tested_combinations"][:n_plain])
 
         roof = stress_roofline(torch, lib, dev, sp)
+        extra = {}
+        if not args.headline_only:
+            extra["batching"] = bench_batching(torch, lib, dev, sp, flush)
+            extra["ml_dem"] = bench_ml(torch, lib, dev, sp, flush)
+            extra["serving"] = bench_serving(lib)
         cpu = cpu_baseline(phase, seconds=args.cpu_seconds) if args.cpu_seconds > 0 else None
 
         out = {
@@ -338,6 +343,7 @@ def run_ours(args):
             "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
             "gpu_launches": 2 * args.steps,
         }
+        out.update(extra)
     if dist:
         dist.barrier()
         dist.destroy_process_group()
@@ -401,6 +407,192 @@ def stress_roofline(torch, lib, dev, sp):
             "frac_fixed_convention": ops_fixed / (search_ms * 1e-3) / peak,
             "fixed_convention": "(w+1)*ceil(R/32) ops per candidate",
             "peak_source": "lop3.b32 issue rate measured on this GPU (grand_measure_int_peak)"}
+
+
+def _time_device(torch, eng, n, d_rec, d_res, sp, flush, steps, warmup, d_sc=0, d_off=0):
+    """Graph-replayed device decode: per-step CUDA-event times with an L2 flush between."""
+    stream = torch.cuda.current_stream()
+    for _ in range(warmup):
+        flush.fill_(1)
+        if eng.decode_device(n, d_rec.data_ptr(), d_res.data_ptr(), sp, d_sc, d_off, True) != 0:
+            raise RuntimeError("device decode failed")
+    if eng.sync_status(sp) != 0:
+        raise RuntimeError("device decode status error")
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(steps)]
+    for i in range(steps):
+        flush.fill_(i & 255)
+        ev[i][0].record(stream)
+        eng.decode_device(n, d_rec.data_ptr(), d_res.data_ptr(), sp, d_sc, d_off, True)
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    if eng.sync_status(sp) != 0:
+        raise RuntimeError("device decode status error")
+    return np.array([a.elapsed_time(b) for a, b in ev])
+
+
+def bench_batching(torch, lib, dev, sp, flush):
+    """configs[3]: 100k shots mixing BB[[72]], [[108]] (W=3), [[144]], [[288]] (W=4) at
+    p = 0.003, shuffled, in one persistent launch (tuned, graph-replayed) vs the plain
+    paths: one C ABI call per code, and one call (one launch pair) per shot."""
+    from library_s_grand_gb300 import autotune, capi, synth
+    from library_s_grand_gb300.engine import Engine, offsets_for
+    spec = [(72, 3), (108, 3), (144, 4), (288, 4)]
+    per = 25000
+    eng = Engine(lib)
+    codes, syns, cfgs = [], [], []
+    for ci, (n, W) in enumerate(spec):
+        c = synth.BB_CODES[n]()
+        cfg = capi.GrandDecoderConfig(W, 256, 0, 64, 10, -1)
+        eng.add_css(c.hx, c.hz, "x", False, cfg)
+        _, s = synth.css_shots(c.hz, per, 0.003, seed=40 + ci)
+        codes.append(c)
+        syns.append(s)
+        cfgs.append(cfg)
+    N = per * len(spec)
+    order = np.random.default_rng(0).permutation(N)
+    sc = np.concatenate([np.full(per, ci, np.int32) for ci in range(len(spec))])[order]
+    rows = [r for s in syns for r in s]
+    rec = np.concatenate([rows[i] for i in order]).astype(np.int32)
+    off = offsets_for(eng.rec_lens, sc)
+    d_rec = torch.from_numpy(rec).to(dev)
+    d_sc = torch.from_numpy(sc).to(dev)
+    d_off = torch.from_numpy(off).to(dev)
+    d_res = torch.empty(N * 72, dtype=torch.uint8, device=dev)
+    best, table = autotune.tune(eng, "bb-mix-100k", N, d_rec.data_ptr(), d_res.data_ptr(), sp,
+                                d_sc.data_ptr(), d_off.data_ptr(), use_cache=False,
+                                grid=[(l, 4, c) for l in (8, 10, 12, 14) for c in (0, 2)])
+    per_step = _time_device(torch, eng, N, d_rec, d_res, sp, flush, 50, 5, d_sc.data_ptr(),
+                            d_off.data_ptr())
+    dev_rate = N / (per_step.mean() * 1e-3)
+    # persistent, host buffers in and out (the engine's public call)
+    eng.decode(rec, sc)
+    t0 = time.perf_counter()
+    reps = 10
+    for _ in range(reps):
+        rc, res_e = eng.decode(rec, sc)
+    e2e_rate = N * reps / (time.perf_counter() - t0)
+    # plain: one upstream-API call per code
+    t0 = time.perf_counter()
+    per_code = []
+    for c, s, cfg in zip(codes, syns, cfgs):
+        rc, r = capi.run_grand_shots_cc(lib, c.hx, c.hz, None, s, cfg, b"x")
+        per_code.append(capi.results_array(r))
+    per_code_rate = N / (time.perf_counter() - t0)
+    ref = np.concatenate(per_code)[order]
+    for f in ("found", "found_weight", "tam", "total_tested_combinations", "iteration"):
+        assert np.array_equal(res_e[f], ref[f]), f
+    # plain: one call per shot, on a sample
+    k = 2000
+    t0 = time.perf_counter()
+    rc, res_p = eng.decode_plain(rec[:int(off[k])], sc[:k])
+    per_shot_rate = k / (time.perf_counter() - t0)
+    assert np.array_equal(res_p["total_tested_combinations"], ref["total_tested_combinations"][:k])
+    return {"workload": "100k shots: BB72/BB108 W=3, BB144/BB288 W=4, p=0.003, shuffled, "
+                        "syndrome records", "shots": N,
+            "persistent_shots_per_s": dev_rate, "persistent_ms_per_batch": float(per_step.mean()),
+            "persistent_e2e_shots_per_s": e2e_rate,
+            "plain_per_code_call_shots_per_s": per_code_rate,
+            "plain_per_shot_call_shots_per_s": per_shot_rate,
+            "persistent_vs_plain_per_code": dev_rate / per_code_rate,
+            "persistent_vs_plain_per_shot": dev_rate / per_shot_rate,
+            "autotune": {"best": {"light_log2": best[0], "tile_k": best[1],
+                                  "search_ctas_per_sm": best[2]},
+                         "table_ms": [[s, round(t, 4)] for s, t in table]},
+            "candidates_per_batch": int(ref["total_tested_combinations"].sum())}
+
+
+def bench_ml(torch, lib, dev, sp, flush):
+    """configs[2]: grand_decode_ML_cln on the 120 x 720 random DEM, 65536 shots, W=3."""
+    from library_s_grand_gb300 import capi, synth
+    from library_s_grand_gb300.engine import Engine
+    dem = synth.random_dem(0)
+    tmp = tempfile.mkdtemp()
+    lf = synth.write_llr_file(os.path.join(tmp, "llr.txt"), dem.llr)
+    n = 65536
+    det, log, _ = synth.dem_shots(dem, n, 1)
+    cfg = capi.GrandDecoderConfig(3, 256, 0, 64, 10, -1)
+    eng = Engine(lib)
+    eng.add_dem(dem.h, dem.l, cfg, 2, lf)
+    rec = np.ascontiguousarray(np.concatenate([det, log], axis=1), dtype=np.int32)
+    d_rec = torch.from_numpy(rec.ravel()).to(dev)
+    d_res = torch.empty(n * 72, dtype=torch.uint8, device=dev)
+    per_step = _time_device(torch, eng, n, d_rec, d_res, sp, flush, 50, 5)
+    res = np.frombuffer(d_res.cpu().numpy().tobytes(), dtype=capi.RESULT_DTYPE)
+    capi.run_grand_ML_shots_cln(lib, dem.h, dem.l, det, log, dem.n_logicos, cfg, lf)
+    t0 = time.perf_counter()
+    reps = 10
+    for _ in range(reps):
+        rc, r = capi.run_grand_ML_shots_cln(lib, dem.h, dem.l, det, log, dem.n_logicos, cfg, lf)
+        assert rc == 0
+    e2e = n * reps / (time.perf_counter() - t0)
+    return {"workload": "grand_decode_ML_cln, random DEM 120 x 720 (column weight 2-4, 12 "
+                        "logicals), p log-uniform [1e-4, 5e-3], 65536 shots, W=3, cap 64",
+            "device_shots_per_s": n / (per_step.mean() * 1e-3),
+            "device_ms_per_batch": float(per_step.mean()), "e2e_shots_per_s": e2e,
+            "found_fraction": float(res["found"].mean()),
+            "logical_success_fraction": float(res["degenerate"].mean()),
+            "candidates_per_batch": int(res["total_tested_combinations"].sum())}
+
+
+def bench_serving(lib):
+    """configs[4]: Poisson arrivals of 1-256-shot requests over four BB codes (W=3,
+    syndrome records) and the 120 x 720 DEM in ML mode, offered load swept to
+    saturation through the continuous-batching server."""
+    from library_s_grand_gb300 import capi, synth
+    from library_s_grand_gb300.engine import Engine
+    from library_s_grand_gb300.server import Server
+    tmp = tempfile.mkdtemp()
+    dem = synth.random_dem(0)
+    lf = synth.write_llr_file(os.path.join(tmp, "llr.txt"), dem.llr)
+    eng = Engine(lib)
+    pools = []
+    for i, nq in enumerate((72, 108, 144, 288)):
+        c = synth.BB_CODES[nq]()
+        eng.add_css(c.hx, c.hz, "x", False, capi.GrandDecoderConfig(3, 256, 0, 64, 10, -1))
+        _, s = synth.css_shots(c.hz, 4096, 0.003, seed=60 + i)
+        pools.append(s)
+    eng.add_dem(dem.h, dem.l, capi.GrandDecoderConfig(3, 256, 0, 64, 10, -1), 2, lf)
+    det, log, _ = synth.dem_shots(dem, 4096, 65)
+    pools.append(np.concatenate([det, log], axis=1).astype(np.int32))
+    rng = np.random.default_rng(7)
+    nreq = 6000
+    sizes = rng.integers(1, 257, size=nreq).astype(np.int32)
+    cids = rng.integers(0, len(pools), size=nreq)
+    recs, scs = [], []
+    for s, c in zip(sizes, cids):
+        start = int(rng.integers(0, 4096 - s))
+        recs.append(pools[c][start:start + s].ravel())
+        scs.append(np.full(s, c, np.int32))
+    rec = np.concatenate(recs).astype(np.int32)
+    sc = np.concatenate(scs)
+    # capacity estimate: everything as one batch
+    eng.decode(rec, sc)
+    t0 = time.perf_counter()
+    rc, ref = eng.decode(rec, sc)
+    cap_req = nreq / (time.perf_counter() - t0)
+    srv = Server(eng, slots=4, max_shots_per_batch=4096)
+    points = []
+    shot0 = np.concatenate([[0], np.cumsum(sizes)])
+    rec0 = np.concatenate([[0], np.cumsum([len(r) for r in recs])])
+    for frac in (0.1, 0.25, 0.5, 0.75, 1.0, 1.5):
+        rate = cap_req * frac
+        k = int(min(nreq, max(400, rate * 0.6)))
+        arrival = np.cumsum(rng.exponential(1.0 / rate, size=k))
+        rc, res, lat, wall = srv.replay(arrival, sizes[:k], rec[:rec0[k]], sc[:shot0[k]])
+        assert rc == 0
+        assert np.array_equal(res["total_tested_combinations"],
+                              ref["total_tested_combinations"][:shot0[k]])
+        points.append({"offered_requests_per_s": rate, "offered_shots_per_s": rate * 128.5,
+                       "requests": k, "achieved_shots_per_s": float(shot0[k] / wall),
+                       "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                       "p999_ms": float(np.percentile(lat, 99.9))})
+    slots, nbytes = srv.info()
+    srv.close()
+    return {"workload": "Poisson arrivals, requests of U{1..256} shots, code uniform over "
+                        "BB72/BB108/BB144/BB288 (W=3, syndrome records) and the 120 x 720 DEM (ML)",
+            "slots": slots, "slot_device_bytes": nbytes, "batch_capacity_requests_per_s": cap_req,
+            "sweep": points}
 
 
 def run_case(args):
@@ -478,6 +670,8 @@ def main():
                     help="profiling mode: run one case --case-reps times, print kernel times")
     ap.add_argument("--case-reps", type=int, default=2)
     ap.add_argument("--case-shots", type=int, default=0)
+    ap.add_argument("--headline-only", action="store_true",
+                    help="skip the batching, ML and serving sections")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.case:
