@@ -227,6 +227,18 @@ def main(ref_dir):
     # mode 1 for the DEM family with every search on upstream's CPU branch
     w.dem("cln_dem120_mode1", O.UNIFORM, dem3, det, log, mk(3, mode=1, cap=30, thr=30),
           keep=cpu_branch_only)
+    # more than 256 detectors: columns wider than 8 words (runtime-width kernels)
+    dem4 = S.random_dem(31, detectors=300, mechanisms=600, logicals=10, p_range=(3e-3, 2e-2))
+    det, log, _ = S.dem_shots(dem4, 250, 32)
+    w.dem("cln_dem300_w3_cap24", O.UNIFORM, dem4, det, log, mk(3, cap=24))
+    w.dem("ml_dem300_w3_cap24", O.ML, dem4, det, log, mk(3, cap=24), llr=dem4.llr)
+    # ML at weight 5 and 6: sub-prefixes of 3-4 elements inside the register-blocked tiles
+    det, log, _ = S.dem_shots(dem, 150, 33)
+    w.dem("ml_dem60_w5_cap24", O.ML, dem, det, log, mk(5, cap=24), llr=dem.llr)
+    w.dem("cln_dem60_w6_cap20", O.UNIFORM, dem, det, log, mk(6, cap=20))
+    # BB[[288]] (5-word columns) random syndromes: exhaustive heavy searches
+    rs = (np.random.default_rng(4).random((2, 144)) < 0.5).astype(np.int32)
+    w.css("cc_bb288_randsyn_w3", O.UNIFORM, bb288, None, rs, mk(3))
 
     with open(os.path.join(OUT, "index.json"), "w", encoding="utf-8") as f:
         json.dump(dict(matrix_sha256=digests, fixtures=w.index), f, indent=1, sort_keys=True)
