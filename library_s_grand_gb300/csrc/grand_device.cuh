@@ -290,11 +290,15 @@ __device__ __forceinline__ void load_words(const uint32_t *col, uint32_t (&a)[NW
   }
 }
 
+// z = OR_i (a[i] ^ T[i]): one lop3 per word.  LUT 0x3C is a ^ b; LUT 0xBE is
+// (a ^ b) | c, so each further word folds its XOR and the running OR together.
 template <int NW>
 __device__ __forceinline__ uint32_t diff_words(const uint32_t (&a)[NW], const uint32_t (&T)[NW]) {
-  uint32_t z = a[0] ^ T[0];
+  uint32_t z;
+  asm("lop3.b32 %0, %1, %2, 0, 0x3C;" : "=r"(z) : "r"(a[0]), "r"(T[0]));
 #pragma unroll
-  for (int i = 1; i < NW; ++i) z |= a[i] ^ T[i];
+  for (int i = 1; i < NW; ++i)
+    asm("lop3.b32 %0, %1, %2, %3, 0xBE;" : "=r"(z) : "r"(a[i]), "r"(T[i]), "r"(z));
   return z;
 }
 
@@ -425,13 +429,10 @@ __device__ __forceinline__ void eval_run_tile(const SegView &sv, const unsigned 
   for (int j = c + 1; j < tam; ++j) {
     uint32_t a[NW];
     load_words<NW>(cols + (size_t)j * nwp, a);
-    if constexpr (KK == 4) {
-      const uint32_t z0 = diff_words<NW>(a, T[0]);
-      const uint32_t z1 = diff_words<NW>(a, T[1]);
-      const uint32_t z2 = diff_words<NW>(a, T[2]);
-      const uint32_t z3 = diff_words<NW>(a, T[3]);
-      acc = __vimin3_u32(acc, z0, z1);
-      acc = __vimin3_u32(acc, z2, z3);
+    if constexpr (KK % 2 == 0) {
+#pragma unroll
+      for (int s = 0; s < KK; s += 2)
+        acc = __vimin3_u32(acc, diff_words<NW>(a, T[s]), diff_words<NW>(a, T[s + 1]));
     } else {
 #pragma unroll
       for (int s = 0; s < KK; ++s) acc = min(acc, diff_words<NW>(a, T[s]));

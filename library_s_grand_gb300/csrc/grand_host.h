@@ -12,9 +12,10 @@
 
 namespace grand {
 
-// Kernel launchers (grand_kernels.cu).
+// Kernel launchers (grand_triage.cu, grand_search.cu).
 cudaError_t launch_triage(const DevBatch &b, int grid, cudaStream_t s);
 cudaError_t launch_search(const DevBatch &b, int grid, cudaStream_t s);
+cudaError_t triage_occupancy(int *blocks_per_sm);
 cudaError_t occupancy(int *triage_blocks_per_sm, int *search_blocks_per_sm);
 
 void set_error(const char *fmt, ...);

@@ -1,0 +1,212 @@
+// grand_kernels.cuh -- what the triage and search kernels share: launch
+// constants, the per-shot result writer, the first-hit winner lookup and the
+// evaluation dispatch on the column word count.  The two kernels live in their
+// own translation units (grand_triage.cu, grand_search.cu) so they compile in
+// parallel.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "grand_device.cuh"
+
+namespace grand {
+
+constexpr int kTriageWarps = 4;
+constexpr int kLightTam = 96;
+constexpr int kLightWords = kLightTam * 8;
+constexpr int kSearchThreads = 256;
+constexpr int kSearchWarps = kSearchThreads / 32;
+constexpr int kWarpStage = 1280;  // staged active-column words per search warp
+constexpr int kTilesPerFetch = 4;
+constexpr int kRunKK = 8;       // prefixes per lane in a run tile (search kernel)
+constexpr int kRunKKLight = 4;  // the same inside the triage warp's light search
+
+// ---------------------------------------------------------------------------
+// Result writer shared by the light path and the search kernel (one warp).
+// ---------------------------------------------------------------------------
+struct Winner {
+  int found;
+  int ii;                   // index into J.it
+  int seg;                  // index into J.seg
+  unsigned long long rank;  // lexicographic rank inside the weight block
+  unsigned long long count; // candidates the winning iteration reports
+  float cost;
+};
+
+static __device__ void finish_shot(const DevBatch &b, const DevCode &cd, const Job &J, int shot,
+                            const Winner &wn, const uint32_t *ebits, uint32_t *delta) {
+  const int lane = threadIdx.x & 31;
+  int p[kMaxW];
+  int w = 0;
+  if (wn.found) {
+    const Seg &S = J.seg[wn.seg];
+    const IterInfo &I = J.it[wn.ii];
+    w = S.w;
+    int c[kMaxW];
+    lex_unrank(b.ncr, wn.rank, I.tam, w, c);
+#pragma unroll
+    for (int i = 0; i < kMaxW; ++i) p[i] = (i < w) ? I.pos[c[i]] : -1;
+  } else {
+#pragma unroll
+    for (int i = 0; i < kMaxW; ++i) p[i] = -1;
+  }
+
+  int degenerate = 0, is_equal = 0;
+  if (wn.found && cd.family == kCss && cd.input_kind == kInErrors) {
+    // is_equal: supplied error == decoded error (grand_decoder.cu:1362).
+    bool eq = true;
+    for (int q = lane; q < cd.mw; q += 32) {
+      uint32_t e = 0;
+#pragma unroll
+      for (int i = 0; i < kMaxW; ++i)
+        if (i < w && (p[i] >> 5) == q) e |= 1u << (p[i] & 31);
+      uint32_t d = ebits[q] ^ e;
+      delta[q] = d;
+      eq = eq && d == 0u;
+    }
+    is_equal = __all_sync(kFull, eq) ? 1 : 0;
+    __syncwarp();
+    // degenerate: (e ^ e_est) in the row space of the other matrix
+    // (grand_decoder.cu:456-474).  In reduced row echelon form the vector's own
+    // bits at pivot columns decide alone which rows upstream adds, so the test
+    // is delta == XOR of the rows pivoted on delta's set bits.
+    uint32_t acc[4] = {0u, 0u, 0u, 0u};  // words lane, lane+32, lane+64, lane+96
+    for (int q = 0; q < cd.mw; ++q) {
+      uint32_t word = delta[q];
+      while (word) {
+        const int c = q * 32 + __ffs(word) - 1;
+        word &= word - 1u;
+        const int r = __ldg(cd.pivrow + c);
+        if (r < 0) continue;
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+          if (lane + 32 * k < cd.mw) acc[k] ^= __ldg(cd.rref + (size_t)r * cd.mw + lane + 32 * k);
+      }
+    }
+    bool ok = true;
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (lane + 32 * k < cd.mw) ok = ok && acc[k] == delta[lane + 32 * k];
+    degenerate = __all_sync(kFull, ok) ? 1 : 0;
+  } else if (wn.found && cd.family == kDem) {
+    // decoded logical flips vs the supplied true flips (grand_decoder.cu:1623-1644)
+    bool eq = true;
+    for (int q = lane; q < cd.nlw; q += 32) {
+      uint32_t le = 0;
+#pragma unroll
+      for (int i = 0; i < kMaxW; ++i)
+        if (i < w) le ^= __ldg(cd.lcols + (size_t)p[i] * cd.nlw + q);
+      eq = eq && le == ebits[q];
+      if (b.dec_log) {
+        for (int j = 0; j < 32 && q * 32 + j < cd.n_logicos; ++j)
+          b.dec_log[(size_t)shot * cd.n_logicos + q * 32 + j] = (unsigned char)((le >> j) & 1u);
+      }
+    }
+    degenerate = __all_sync(kFull, eq) ? 1 : 0;
+  } else if (cd.family == kDem && b.dec_log) {
+    for (int j = lane; j < cd.n_logicos; j += 32) b.dec_log[(size_t)shot * cd.n_logicos + j] = 0;
+  }
+
+  if (b.dec_err) {
+    for (int c = lane; c < cd.m; c += 32) {
+      unsigned char v = 0;
+#pragma unroll
+      for (int i = 0; i < kMaxW; ++i)
+        if (i < w && p[i] == c) v = 1;
+      b.dec_err[(size_t)shot * cd.m + c] = v;
+    }
+  }
+
+  if (lane == 0) {
+    int h = -2;
+    unsigned long long tested = 0;
+    const int last = wn.found ? wn.ii : J.n_it - 1;
+    for (int k = 0; k <= last; ++k) {
+      h = (J.it[k].branch == kBranchGpu) ? (h == -1 ? 1 : 0) : -1;
+      if (k < last || !wn.found) tested += J.it[k].total;
+    }
+    if (wn.found) tested += wn.count;
+    GrandDecoderResult r;
+    r.found = wn.found;
+    r.found_weight = w;
+    r.original_weight = J.original_weight;
+    r.degenerate = degenerate;
+    r.is_equal = is_equal;
+    r.tam = wn.found ? J.it[wn.ii].tam : J.final_tam;
+    r.total_tested_combinations = tested;
+    r.hibrido = h;
+    r.iteration = wn.found ? J.it[wn.ii].it : J.final_iteration;
+    r.time_sum_ms = 0.0;
+    r.total_time_search_ms = 0.0;
+    r.transfer_time_ms = 0.0;
+    r.total_to_find_ms = 0.0;
+    b.results[shot] = r;
+    if (b.ml_cost) b.ml_cost[shot] = wn.found ? wn.cost : 0.0f;
+    if (J.failed) atomicOr(b.status, kStatusTamLimit);
+  }
+}
+
+// Winner of a first-hit search from the lowest matching global index.
+static __device__ Winner winner_from_index(const Job &J, unsigned long long g, bool prob) {
+  Winner wn;
+  wn.found = 0;
+  wn.ii = wn.seg = 0;
+  wn.rank = wn.count = 0;
+  wn.cost = 0.0f;
+  if (g == kNone) return wn;
+  for (int ii = 0; ii < J.n_it; ++ii) {
+    const IterInfo &I = J.it[ii];
+    if (g < I.base || g >= I.base + I.total) continue;
+    for (int s = I.seg_lo; s < I.seg_hi; ++s) {
+      const Seg &S = J.seg[s];
+      if (S.dup || g < S.base || g >= S.base + S.count) continue;
+      wn.found = 1;
+      wn.ii = ii;
+      wn.seg = s;
+      wn.rank = g - S.base;
+      if (I.branch == kBranchCpu) wn.count = g - I.base + 1ull;  // grand_decoder.cu:547-548
+      else if (prob) wn.count = I.phase_end[S.phase];            // grand_decoder.cu:1006
+      else wn.count = I.total;                                   // grand_decoder.cu:1303-1304
+      return wn;
+    }
+  }
+  return wn;
+}
+
+// ---------------------------------------------------------------------------
+// Evaluation dispatch on the column word count.
+// ---------------------------------------------------------------------------
+template <bool ML>
+__device__ __forceinline__ void eval_dispatch(int nw, const SegView &sv,
+                                              const unsigned long long *t, const uint32_t *sw,
+                                              unsigned long long tile, LaneBest &lb) {
+  switch (nw) {
+    case 1: eval_tile<1, ML>(sv, t, sw, tile, lb); break;
+    case 2: eval_tile<2, ML>(sv, t, sw, tile, lb); break;
+    case 3: eval_tile<3, ML>(sv, t, sw, tile, lb); break;
+    case 4: eval_tile<4, ML>(sv, t, sw, tile, lb); break;
+    case 5: eval_tile<5, ML>(sv, t, sw, tile, lb); break;
+    case 6: eval_tile<6, ML>(sv, t, sw, tile, lb); break;
+    case 7: eval_tile<7, ML>(sv, t, sw, tile, lb); break;
+    case 8: eval_tile<8, ML>(sv, t, sw, tile, lb); break;
+    default: eval_tile<0, ML>(sv, t, sw, tile, lb); break;
+  }
+}
+
+template <bool ML, int KK>
+__device__ __forceinline__ void eval_run_dispatch(int nw, const SegView &sv,
+                                                  const unsigned long long *t, const uint32_t *sw,
+                                                  int c, unsigned long long r0, LaneBest &lb) {
+  switch (nw) {
+    case 1: eval_run_tile<1, KK, ML>(sv, t, sw, c, r0, lb); break;
+    case 2: eval_run_tile<2, KK, ML>(sv, t, sw, c, r0, lb); break;
+    case 3: eval_run_tile<3, KK, ML>(sv, t, sw, c, r0, lb); break;
+    case 4: eval_run_tile<4, KK, ML>(sv, t, sw, c, r0, lb); break;
+    case 5: eval_run_tile<5, KK, ML>(sv, t, sw, c, r0, lb); break;
+    case 6: eval_run_tile<6, KK, ML>(sv, t, sw, c, r0, lb); break;
+    case 7: eval_run_tile<7, KK, ML>(sv, t, sw, c, r0, lb); break;
+    default: eval_run_tile<8, KK, ML>(sv, t, sw, c, r0, lb); break;
+  }
+}
+
+}  // namespace grand

@@ -1,0 +1,251 @@
+// grand_search.cu -- kernel 2 of a decoding launch (sm_103a).
+//
+// search_kernel (persistent, every warp an independent worker)
+//   every warp repeatedly takes the next tiles (K colex prefixes per lane of
+//   one weight block of one Job) from a global counter, stages the iteration's
+//   active columns in its own shared-memory slice, evaluates them, publishes
+//   the lowest matching global index (atomicMin) or the lowest {cost, rank}
+//   key (128-bit CAS), and the warp that completes a Job's last tile writes its
+//   result.  Tiles whose candidates all rank above an already-found match are
+//   skipped.  No warp ever waits for another: there are no block barriers.
+#include "grand_host.h"
+#include "grand_kernels.cuh"
+
+namespace grand {
+
+// ---------------------------------------------------------------------------
+// Kernel 2: persistent work-stealing search over the Jobs' tiles.
+// ---------------------------------------------------------------------------
+__device__ bool tile_skip(const Job &J, const Seg &S, const IterInfo &I, bool ml) {
+  if (!ml) {
+    const unsigned long long best = *reinterpret_cast<const volatile unsigned long long *>(&J.best);
+    return S.base >= best;
+  }
+  for (int i = 0; i < S.iter; ++i)
+    for (int w = 1; w <= kMaxW; ++w)
+      if (*reinterpret_cast<const volatile unsigned long long *>(&J.mlkey[i][w][0]) != kNone)
+        return true;
+  for (int w = 1; w < S.w; ++w) {
+    const unsigned long long o =
+        *reinterpret_cast<const volatile unsigned long long *>(&J.mlkey[S.iter][w][0]);
+    if (o != kNone && I.prefix[S.w] >= key_cost((uint32_t)o)) return true;
+  }
+  return false;
+}
+
+__device__ Winner winner_ml(const Job &J) {
+  Winner wn;
+  wn.found = 0;
+  wn.ii = wn.seg = 0;
+  wn.rank = wn.count = 0;
+  wn.cost = 0.0f;
+  for (int ii = J.it_lo; ii < J.n_it; ++ii) {
+    const IterInfo &I = J.it[ii];
+    uint32_t bo = 0xffffffffu;
+    unsigned long long br = kNone, proc = 0;
+    int bseg = -1;
+    for (int s = I.seg_lo; s < I.seg_hi; ++s) {
+      const Seg &S = J.seg[s];
+      if (bseg >= 0 && I.prefix[S.w] >= key_cost(bo)) break;
+      proc += S.count;
+      const unsigned long long o = J.mlkey[ii][S.w][0];
+      if (o != kNone && (bseg < 0 || (uint32_t)o < bo)) {
+        bo = (uint32_t)o;
+        br = J.mlkey[ii][S.w][1];
+        bseg = s;
+      }
+    }
+    if (bseg >= 0) {
+      wn.found = 1;
+      wn.ii = ii;
+      wn.seg = bseg;
+      wn.rank = br;
+      wn.count = (I.branch == kBranchCpu) ? proc : I.total;
+      wn.cost = key_cost(bo);
+      return wn;
+    }
+  }
+  return wn;
+}
+
+__global__ void __launch_bounds__(kSearchThreads, 3) search_kernel(DevBatch b) {
+  __shared__ __align__(16) uint32_t s_stage[kSearchWarps][kWarpStage];
+  __shared__ uint32_t s_sw[kSearchWarps][kMaxRows / 32];
+  __shared__ uint32_t s_delta[kSearchWarps][kMaxCols / 32];
+
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  uint32_t *stage = s_stage[warp];
+  uint32_t *sw = s_sw[warp];
+  const unsigned long long packed = *reinterpret_cast<volatile unsigned long long *>(b.counters);
+  unsigned long long njobs = packed >> 40;
+  unsigned long long total = packed & ((1ull << 40) - 1ull);
+  if (njobs > (unsigned long long)b.max_jobs) {
+    njobs = b.max_jobs;
+    total = njobs ? b.jobs[njobs - 1].tile_base + b.jobs[njobs - 1].ntiles : 0ull;
+  }
+  int st_job = -1, st_it = -1;
+  // per-warp caches of the last job / weight block / run looked up, and a
+  // register copy of the current weight block's parameters
+  int cj = -1, cs = -1, cc = -1;
+  unsigned long long cj_lo = 0, cj_hi = 0, cs_lo = 0, cs_hi = 0, cc_lo = 0, cc_hi = 0;
+  Job *Jp = nullptr;
+  const DevCode *cdp = nullptr;
+  SegView sv{};
+  int s_runs = 0, s_iter = 0, s_ml = 0, s_prob = 0, s_nw = 0;
+  const unsigned long long *s_cum = nullptr;
+
+  for (;;) {
+    unsigned long long t0 = 0;
+    if (lane == 0) t0 = atomicAdd(&b.counters[1], (unsigned long long)kTilesPerFetch);
+    t0 = __shfl_sync(kFull, t0, 0);
+    if (t0 >= total) break;
+    const unsigned long long t1 = (t0 + kTilesPerFetch < total) ? t0 + kTilesPerFetch : total;
+    bool skip_known = false, skip = false;
+    unsigned long long pending = 0;
+    bool fenced = false;
+    for (unsigned long long t = t0; t < t1; ++t) {
+      if (cj < 0 || t < cj_lo || t >= cj_hi) {
+        int lo = 0, hi = (int)njobs - 1;
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (b.jobs[mid].tile_base <= t) lo = mid;
+          else hi = mid - 1;
+        }
+        cj = lo;
+        Jp = &b.jobs[lo];
+        cdp = &b.codes[Jp->code];
+        cj_lo = Jp->tile_base;
+        cj_hi = cj_lo + Jp->ntiles;
+        cs = -1;
+      }
+      Job &J = *Jp;
+      const unsigned long long lt = t - cj_lo;
+      if (cs < 0 || lt < cs_lo || lt >= cs_hi) {
+        int sg = 0;
+        while (sg < J.nseg - 1 &&
+               !(J.seg[sg].njt && lt >= J.seg[sg].tile_lo && lt < J.seg[sg].tile_lo + J.seg[sg].njt))
+          ++sg;
+        const Seg &S = J.seg[sg];
+        const IterInfo &I = J.it[S.iter];
+        cs = sg;
+        cs_lo = S.tile_lo;
+        cs_hi = cs_lo + S.njt;
+        cc = -1;
+        s_runs = S.runs;
+        s_cum = S.cum;
+        s_iter = S.iter;
+        s_nw = cdp->nw;
+        s_ml = cdp->variant == kMl;
+        s_prob = cdp->variant == kProb;
+        const bool staged = I.tam * cdp->nwp <= kWarpStage;
+        sv = SegView{staged ? stage : I.cols, I.llr, I.tam, S.w, S.K, cdp->nwp, cdp->nw,
+                     S.nprefix, S.base};
+        if (st_job != cj || st_it != S.iter) {
+          __syncwarp();
+          if (staged) {
+            const uint4 *src = reinterpret_cast<const uint4 *>(I.cols);
+            uint4 *dst = reinterpret_cast<uint4 *>(stage);
+            const int n4 = (I.tam * cdp->nwp + 3) / 4;
+            for (int i = lane; i < n4; i += 32) dst[i] = src[i];
+          }
+          sw[lane] = J.sw[lane];
+          __syncwarp();
+          st_job = cj;
+          st_it = S.iter;
+        }
+        skip_known = false;
+      }
+      if (!skip_known || s_ml) {
+        skip = tile_skip(J, J.seg[cs], J.it[s_iter], s_ml);
+        skip_known = true;
+      }
+      bool published = false;
+      if (!skip) {
+        LaneBest lb;
+        lb.reset();
+        const unsigned long long st = lt - cs_lo;
+        if (s_runs) {
+          if (cc < 0 || st < cc_lo || st >= cc_hi) {
+            // run c holding segment tile st: largest c with cum[c] <= st
+            int clo = 0, chi = sv.tam - 2;
+            while (clo < chi) {
+              const int mid = (clo + chi + 1) >> 1;
+              if (s_cum[mid] <= st) clo = mid;
+              else chi = mid - 1;
+            }
+            cc = clo;
+            cc_lo = s_cum[clo];
+            cc_hi = cc_lo + run_tiles(b.ncr, clo, sv.w, kRunKK);
+          }
+          const unsigned long long r0 = (st - cc_lo) * (32ull * kRunKK);
+          if (s_ml) eval_run_dispatch<true, kRunKK>(s_nw, sv, b.ncr, sw, cc, r0, lb);
+          else eval_run_dispatch<false, kRunKK>(s_nw, sv, b.ncr, sw, cc, r0, lb);
+        } else {
+          if (s_ml) eval_dispatch<true>(s_nw, sv, b.ncr, sw, st, lb);
+          else eval_dispatch<false>(s_nw, sv, b.ncr, sw, st, lb);
+        }
+        if (!s_ml) {
+          const unsigned long long g = warp_min_u64(lb.g);
+          if (g != kNone) {
+            published = true;
+            skip_known = false;
+            if (lane == 0) atomicMin(&J.best, g);
+          }
+        } else {
+          uint32_t o = lb.o;
+          unsigned long long r = lb.r;
+          warp_min_key(o, r);
+          if (o != 0xffffffffu) {
+            published = true;
+            if (lane == 0 && !atomic_min_key(J.mlkey[s_iter][sv.w], o, r))
+              atomicOr(b.status, kStatusCasLimit);
+          }
+        }
+      }
+      // tiles of this fetch done for the current job: posted once per job per fetch
+      pending += 1ull;
+      fenced = fenced || published;
+      const bool flush = (t + 1 == t1) || (t + 1 >= cj_hi);
+      if (flush) {
+        int last = 0;
+        if (lane == 0) {
+          if (fenced) __threadfence();  // order the published minima before the count
+          last = (atomicAdd(&J.tiles_done, pending) + pending == J.ntiles) ? 1 : 0;
+        }
+        pending = 0;
+        fenced = false;
+        last = __shfl_sync(kFull, last, 0);
+        if (last) {
+          __threadfence();
+          Winner wn;
+          if (!s_ml)
+            wn = winner_from_index(J, *reinterpret_cast<volatile unsigned long long *>(&J.best),
+                                   s_prob != 0);
+          else
+            wn = winner_ml(J);
+          finish_shot(b, *cdp, J, J.shot, wn, J.ebits, s_delta[warp]);
+        }
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host-callable launcher.
+// ---------------------------------------------------------------------------
+cudaError_t launch_search(const DevBatch &b, int grid, cudaStream_t s) {
+  search_kernel<<<grid, kSearchThreads, 0, s>>>(b);
+  return cudaGetLastError();
+}
+
+int search_threads_per_block() { return kSearchThreads; }
+
+cudaError_t occupancy(int *triage_blocks_per_sm, int *search_blocks_per_sm) {
+  cudaError_t e = triage_occupancy(triage_blocks_per_sm);
+  if (e != cudaSuccess) return e;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(search_blocks_per_sm, search_kernel,
+                                                       kSearchThreads, 0);
+}
+
+}  // namespace grand
