@@ -129,24 +129,6 @@ bool verbose() {
   return v != 0;
 }
 
-// Batch times apportioned to the shots that were searched (upstream reports
-// per-shot timers; shots with an empty syndrome report zeros, as upstream).
-void fill_times(GrandDecoderResult *res, int N, const BatchTiming &t) {
-  int searched = 0;
-  for (int i = 0; i < N; ++i) searched += res[i].hibrido != -2 || res[i].iteration != 0;
-  const double per_sum = searched ? t.triage_ms / searched : 0.0;
-  const double per_search = searched ? t.search_ms / searched : 0.0;
-  const double per_xfer = searched ? (double)(t.h2d_ms + t.d2h_ms) / searched : 0.0;
-  for (int i = 0; i < N; ++i) {
-    GrandDecoderResult &r = res[i];
-    if (r.hibrido == -2 && r.iteration == 0) continue;
-    r.time_sum_ms = per_sum;
-    r.total_time_search_ms = per_search;
-    r.transfer_time_ms = per_xfer;
-    r.total_to_find_ms = r.found ? per_search : 0.0;
-  }
-}
-
 void print_css(const GrandDecoderResult *res, int N, bool with_errors) {
   for (int i = 0; i < N; ++i) {
     const GrandDecoderResult *r = &res[i];
@@ -260,10 +242,8 @@ int decode_css(int variant, const int *Hx, const int *Hz, int n, int m, const in
   req.h_results = results;
   req.h_dec_err = out ? out->decoded_errors : nullptr;
   req.dec_m = m;
-  BatchTiming t;
-  int rc = run_batch(ctx, g.w, req, &t);
+  int rc = run_batch(ctx, g.w, req, nullptr);
   if (rc != 0 && rc != GRAND_ERR_LIMIT) return rc;
-  fill_times(results, num_shots, t);
   if (verbose()) print_css(results, num_shots, errors != nullptr);
   return rc;
 }
@@ -344,12 +324,10 @@ int decode_dem(int variant, const int *H, const int *L, int n, int m, int nl, co
   req.h_cost = (out && variant == kMl) ? out->ml_cost : nullptr;
   req.dec_m = m;
   req.dec_nl = nl;
-  BatchTiming t;
-  int rc = run_batch(ctx, g.w, req, &t);
+  int rc = run_batch(ctx, g.w, req, nullptr);
   if (rc != 0 && rc != GRAND_ERR_LIMIT) return rc;
   if (out && variant != kMl && out->ml_cost)
     for (int i = 0; i < num_shots; ++i) out->ml_cost[i] = 0.0f;
-  fill_times(results, num_shots, t);
   if (verbose()) print_dem(results, num_shots);
   return rc;
 }

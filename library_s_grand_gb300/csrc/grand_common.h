@@ -111,6 +111,8 @@ struct alignas(16) Job {
   unsigned long long tiles_done;
   int original_weight;
   int failed;                     // an active set exceeded the kernel limits
+  unsigned long long t_start;     // %globaltimer (ns) when the shot's triage began,
+  unsigned long long t_counts;    //   and when its flagged-check counts were done
   uint32_t *ebits;                // mw words: supplied error (CSS) / truth logicals (DEM)
   uint32_t sw[kMaxRows / 32];     // syndrome bits
   IterInfo it[kMaxIters];
@@ -137,7 +139,8 @@ struct DevBatch {
   const unsigned long long *ncr; // (kMaxTam + 1) x (kMaxW + 1)
   Job *jobs;
   int max_jobs;
-  unsigned long long *counters;  // [0] packed job/tile append, [1] next tile, [2] scratch top
+  unsigned long long *counters;  // [0] packed job/tile append, [1] next tile, [2] scratch top,
+                                 // [3] next shot slot (triage)
   uint32_t *scratch;
   unsigned long long scratch_words;
   unsigned *status;

@@ -25,6 +25,13 @@ namespace grand {
 constexpr unsigned kFull = 0xffffffffu;
 constexpr unsigned long long kNone = ~0ull;
 
+// Nanoseconds of the GPU's global timer (the per-shot timing fields).
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
 __device__ __forceinline__ unsigned long long ncr(const unsigned long long *t, int n, int k) {
   if (n < 0 || k < 0 || n > kMaxTam || k > kMaxW) return 0ull;
   return __ldg(t + n * (kMaxW + 1) + k);

@@ -70,6 +70,7 @@ Workspace::~Workspace() {
                   d_deferred, d_map, d_codes, d_llr, d_off, d_shotcode};
   for (void *b : bufs) cudaFree(b);
   if (h_codes) cudaFreeHost(h_codes);
+  if (h_status) cudaFreeHost(h_status);
   for (auto &e : ev) if (e) cudaEventDestroy(e);
   if (stream) cudaStreamDestroy(stream);
 }
@@ -162,6 +163,12 @@ Workspace *Context::acquire() {
       delete w;
       return nullptr;
     }
+  if (cudaHostAlloc(reinterpret_cast<void **>(&w->h_status), 256, cudaHostAllocDefault) !=
+      cudaSuccess) {
+    w->h_status = nullptr;
+    delete w;
+    return nullptr;
+  }
   return w;
 }
 
@@ -357,7 +364,6 @@ int run_batch(Context *ctx, Workspace *ws, const BatchRequest &req, BatchTiming 
   // Zero-copy: the GPU reads the caller's records and writes its results in
   // place, over NVLink-C2C, when the device can access pageable host memory.
   const bool zc = tn.zero_copy && ctx->pageable_access;
-  CK(ensure(&ws->d_codes, &ws->cap_codes, sizeof(DevCode) * ncodes));
   if (!zc) {
     CK(ensure(&ws->d_in, &ws->cap_in, req.in_ints * sizeof(int)));
     if (req.h_in_log) CK(ensure(&ws->d_in2, &ws->cap_in2, req.in_log_ints * sizeof(int)));
@@ -376,8 +382,16 @@ int run_batch(Context *ctx, Workspace *ws, const BatchRequest &req, BatchTiming 
   CK(ensure(&ws->d_small, &small_cap, 256));
   CK(ensure(&ws->d_deferred, &ws->cap_deferred, sizeof(int) * N));
 
+  // Per-call host work is kept to the launches, one status read and one
+  // synchronisation; events are recorded only when the caller asks for times,
+  // and the DevCode array is uploaded only when it differs from the last one.
+  const bool timed = timing != nullptr;
   const size_t code_bytes = sizeof(DevCode) * ncodes;
-  if (ws->cap_hcodes < code_bytes) {
+  void *codes_before = ws->d_codes;
+  CK(ensure(&ws->d_codes, &ws->cap_codes, code_bytes));
+  const bool send_codes = ws->d_codes != codes_before || ws->sent_codes.size() != code_bytes ||
+                          memcmp(ws->sent_codes.data(), req.codes.data(), code_bytes) != 0;
+  if (send_codes && ws->cap_hcodes < code_bytes) {
     // the previous copy from this buffer may still be in flight on this stream
     CK(cudaStreamSynchronize(s));
     if (ws->h_codes) cudaFreeHost(ws->h_codes);
@@ -386,9 +400,13 @@ int run_batch(Context *ctx, Workspace *ws, const BatchRequest &req, BatchTiming 
     CK(cudaHostAlloc(&ws->h_codes, std::max<size_t>(code_bytes, 4096), cudaHostAllocDefault));
     ws->cap_hcodes = std::max<size_t>(code_bytes, 4096);
   }
-  memcpy(ws->h_codes, req.codes.data(), code_bytes);  // stream is idle between calls
-  CK(cudaEventRecord(ws->ev[0], s));
-  CK(cudaMemcpyAsync(ws->d_codes, ws->h_codes, code_bytes, cudaMemcpyHostToDevice, s));
+  if (timed) CK(cudaEventRecord(ws->ev[0], s));
+  if (send_codes) {
+    memcpy(ws->h_codes, req.codes.data(), code_bytes);  // stream is idle between calls
+    CK(cudaMemcpyAsync(ws->d_codes, ws->h_codes, code_bytes, cudaMemcpyHostToDevice, s));
+    ws->sent_codes.assign(reinterpret_cast<const unsigned char *>(req.codes.data()),
+                          reinterpret_cast<const unsigned char *>(req.codes.data()) + code_bytes);
+  }
   if (!zc) {
     CK(cudaMemcpyAsync(ws->d_in, req.h_in, req.in_ints * sizeof(int), cudaMemcpyHostToDevice, s));
     if (req.h_in_log)
@@ -400,7 +418,7 @@ int run_batch(Context *ctx, Workspace *ws, const BatchRequest &req, BatchTiming 
       CK(cudaMemcpyAsync(ws->d_shotcode, req.h_shot_code, sizeof(int) * N,
                          cudaMemcpyHostToDevice, s));
   }
-  CK(cudaEventRecord(ws->ev[1], s));
+  if (timed) CK(cudaEventRecord(ws->ev[1], s));
 
   DevBatch b;
   memset(&b, 0, sizeof(b));
@@ -444,17 +462,19 @@ int run_batch(Context *ctx, Workspace *ws, const BatchRequest &req, BatchTiming 
   for (;;) {
     b.num_shots = todo;
     b.shot_map = rounds == 0 ? nullptr : (const int *)ws->d_map;
-    CK(cudaEventRecord(ws->ev[2], s));
-    CK(launch_pipeline(ctx, b, tn, s, ws->ev[3]));
-    CK(cudaEventRecord(ws->ev[4], s));
-    unsigned st = 0;
-    CK(cudaMemcpyAsync(&st, b.status, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    if (timed) CK(cudaEventRecord(ws->ev[2], s));
+    CK(launch_pipeline(ctx, b, tn, s, timed ? ws->ev[3] : nullptr));
+    if (timed) CK(cudaEventRecord(ws->ev[4], s));
+    CK(cudaMemcpyAsync(ws->h_status, b.status, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
-    float a = 0, c = 0;
-    cudaEventElapsedTime(&a, ws->ev[2], ws->ev[3]);
-    cudaEventElapsedTime(&c, ws->ev[3], ws->ev[4]);
-    tri_ms += a;
-    sea_ms += c;
+    const unsigned st = *ws->h_status;
+    if (timed) {
+      float a = 0, c = 0;
+      cudaEventElapsedTime(&a, ws->ev[2], ws->ev[3]);
+      cudaEventElapsedTime(&c, ws->ev[3], ws->ev[4]);
+      tri_ms += a;
+      sea_ms += c;
+    }
     ++rounds;
     status_all |= st;
     if (!(st & (kStatusJobOverflow | kStatusScratchOverflow))) break;
@@ -474,7 +494,7 @@ int run_batch(Context *ctx, Workspace *ws, const BatchRequest &req, BatchTiming 
     CK(cudaMemcpyAsync(ws->d_map, map.data(), sizeof(int) * map.size(), cudaMemcpyHostToDevice, s));
   }
 
-  CK(cudaEventRecord(ws->ev[4], s));
+  if (timed) CK(cudaEventRecord(ws->ev[4], s));
   if (!zc) {
     CK(cudaMemcpyAsync(req.h_results, ws->d_res, sizeof(GrandDecoderResult) * N,
                        cudaMemcpyDeviceToHost, s));
@@ -486,12 +506,12 @@ int run_batch(Context *ctx, Workspace *ws, const BatchRequest &req, BatchTiming 
     if (req.h_cost)
       CK(cudaMemcpyAsync(req.h_cost, ws->d_cost, sizeof(float) * N, cudaMemcpyDeviceToHost, s));
   }
-  CK(cudaEventRecord(ws->ev[5], s));
-  CK(cudaStreamSynchronize(s));
-  float h2d = 0, d2h = 0;
-  cudaEventElapsedTime(&h2d, ws->ev[0], ws->ev[1]);
-  cudaEventElapsedTime(&d2h, ws->ev[4], ws->ev[5]);
+  if (timed) CK(cudaEventRecord(ws->ev[5], s));
+  if (!zc || timed) CK(cudaStreamSynchronize(s));
   if (timing) {
+    float h2d = 0, d2h = 0;
+    cudaEventElapsedTime(&h2d, ws->ev[0], ws->ev[1]);
+    cudaEventElapsedTime(&d2h, ws->ev[4], ws->ev[5]);
     timing->h2d_ms = h2d;
     timing->triage_ms = tri_ms;
     timing->search_ms = sea_ms;

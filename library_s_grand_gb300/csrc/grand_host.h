@@ -69,6 +69,8 @@ struct Workspace {
   void *d_map = nullptr; size_t cap_map = 0;
   void *d_codes = nullptr; size_t cap_codes = 0;
   void *h_codes = nullptr; size_t cap_hcodes = 0;  // pinned staging of the DevCode array
+  std::vector<unsigned char> sent_codes;           // DevCode bytes now in d_codes
+  unsigned *h_status = nullptr;                    // pinned: the launch status word
   void *d_llr = nullptr; size_t cap_llr = 0;
   void *d_off = nullptr; size_t cap_off = 0;
   void *d_shotcode = nullptr; size_t cap_shotcode = 0;

@@ -136,10 +136,16 @@ static __device__ void finish_shot(const DevBatch &b, const DevCode &cd, const J
     r.total_tested_combinations = tested;
     r.hibrido = h;
     r.iteration = wn.found ? J.it[wn.ii].it : J.final_iteration;
-    r.time_sum_ms = 0.0;
-    r.total_time_search_ms = 0.0;
+    // Per-shot times from the global timer: the flagged-check count step, the
+    // search from its end to this result (light search, plus queueing and the
+    // search kernel for a published Job), and, when found, the whole shot.
+    // Records move in one batch (or are read in place), so no copy time is
+    // attributed to a shot.
+    const unsigned long long now = global_ns();
+    r.time_sum_ms = 1e-6 * (double)(J.t_counts - J.t_start);
+    r.total_time_search_ms = 1e-6 * (double)(now - J.t_counts);
     r.transfer_time_ms = 0.0;
-    r.total_to_find_ms = 0.0;
+    r.total_to_find_ms = wn.found ? 1e-6 * (double)(now - J.t_start) : 0.0;
     b.results[shot] = r;
     if (b.ml_cost) b.ml_cost[shot] = wn.found ? wn.cost : 0.0f;
     if (J.failed) atomicOr(b.status, kStatusTamLimit);

@@ -16,6 +16,23 @@ namespace grand {
 // ---------------------------------------------------------------------------
 // Kernel 2: persistent work-stealing search over the Jobs' tiles.
 // ---------------------------------------------------------------------------
+// Largest i in [lo, hi] with key(i) <= x, for key non-decreasing and
+// key(lo) <= x.  Each step the 32 lanes probe 32 points of the range, so n
+// entries take ceil(log32 n) dependent loads instead of log2 n.
+template <class Key>
+__device__ __forceinline__ int warp_search_le(int lo, int hi, unsigned long long x, Key key) {
+  const int lane = threadIdx.x & 31;
+  while (lo < hi) {
+    const long long span = (long long)hi - lo + 1;
+    const unsigned m = __ballot_sync(kFull, key(lo + (int)((lane * span) >> 5)) <= x);
+    const int l = 31 - __clz(m);  // lane 0 probes lo, so m != 0
+    const int nlo = lo + (int)((l * span) >> 5);
+    hi = (l == 31) ? hi : lo + (int)(((l + 1) * span) >> 5) - 1;
+    lo = nlo;
+  }
+  return lo;
+}
+
 __device__ bool tile_skip(const Job &J, const Seg &S, const IterInfo &I, bool ml) {
   if (!ml) {
     const unsigned long long best = *reinterpret_cast<const volatile unsigned long long *>(&J.best);
@@ -95,23 +112,24 @@ __global__ void __launch_bounds__(kSearchThreads, 3) search_kernel(DevBatch b) {
   int s_runs = 0, s_iter = 0, s_ml = 0, s_prob = 0, s_nw = 0;
   const unsigned long long *s_cum = nullptr;
 
+  // Tiles are drawn kTilesPerFetch at a time when there are many per warp, one
+  // at a time when there are few, so that a handful of expensive Jobs still
+  // spread over every warp.
+  const unsigned long long fetch =
+      total >= 8ull * kTilesPerFetch * gridDim.x * kSearchWarps ? kTilesPerFetch : 1ull;
   for (;;) {
     unsigned long long t0 = 0;
-    if (lane == 0) t0 = atomicAdd(&b.counters[1], (unsigned long long)kTilesPerFetch);
+    if (lane == 0) t0 = atomicAdd(&b.counters[1], fetch);
     t0 = __shfl_sync(kFull, t0, 0);
     if (t0 >= total) break;
-    const unsigned long long t1 = (t0 + kTilesPerFetch < total) ? t0 + kTilesPerFetch : total;
+    const unsigned long long t1 = (t0 + fetch < total) ? t0 + fetch : total;
     bool skip_known = false, skip = false;
     unsigned long long pending = 0;
     bool fenced = false;
     for (unsigned long long t = t0; t < t1; ++t) {
       if (cj < 0 || t < cj_lo || t >= cj_hi) {
-        int lo = 0, hi = (int)njobs - 1;
-        while (lo < hi) {
-          const int mid = (lo + hi + 1) >> 1;
-          if (b.jobs[mid].tile_base <= t) lo = mid;
-          else hi = mid - 1;
-        }
+        const int lo = warp_search_le(0, (int)njobs - 1, t,
+                                      [&](int j) { return b.jobs[j].tile_base; });
         cj = lo;
         Jp = &b.jobs[lo];
         cdp = &b.codes[Jp->code];
@@ -122,10 +140,20 @@ __global__ void __launch_bounds__(kSearchThreads, 3) search_kernel(DevBatch b) {
       Job &J = *Jp;
       const unsigned long long lt = t - cj_lo;
       if (cs < 0 || lt < cs_lo || lt >= cs_hi) {
-        int sg = 0;
-        while (sg < J.nseg - 1 &&
-               !(J.seg[sg].njt && lt >= J.seg[sg].tile_lo && lt < J.seg[sg].tile_lo + J.seg[sg].njt))
-          ++sg;
+        // the weight block holding job tile lt: every lane tests one block
+        const int nseg = J.nseg;
+        int sg = -1;
+        for (int i0 = 0; i0 < nseg && sg < 0; i0 += 32) {
+          bool hit = false;
+          if (i0 + lane < nseg) {
+            const Seg &C = J.seg[i0 + lane];
+            const unsigned long long njt = C.njt, tlo = C.tile_lo;
+            hit = njt && lt >= tlo && lt < tlo + njt;
+          }
+          const unsigned m = __ballot_sync(kFull, hit);
+          if (m) sg = i0 + __ffs(m) - 1;
+        }
+        if (sg < 0) sg = nseg - 1;
         const Seg &S = J.seg[sg];
         const IterInfo &I = J.it[S.iter];
         cs = sg;
@@ -168,12 +196,8 @@ __global__ void __launch_bounds__(kSearchThreads, 3) search_kernel(DevBatch b) {
         if (s_runs) {
           if (cc < 0 || st < cc_lo || st >= cc_hi) {
             // run c holding segment tile st: largest c with cum[c] <= st
-            int clo = 0, chi = sv.tam - 2;
-            while (clo < chi) {
-              const int mid = (clo + chi + 1) >> 1;
-              if (s_cum[mid] <= st) clo = mid;
-              else chi = mid - 1;
-            }
+            const unsigned long long *cum = s_cum;
+            const int clo = warp_search_le(0, sv.tam - 2, st, [&](int i) { return cum[i]; });
             cc = clo;
             cc_lo = s_cum[clo];
             cc_hi = cc_lo + run_tiles(b.ncr, clo, sv.w, kRunKK);
@@ -218,13 +242,23 @@ __global__ void __launch_bounds__(kSearchThreads, 3) search_kernel(DevBatch b) {
         last = __shfl_sync(kFull, last, 0);
         if (last) {
           __threadfence();
+          // The Job as the other warps left it, read from L2 (past this SM's
+          // L1) into this warp's stage in one pass, so the winner lookup and
+          // the result writer walk shared memory instead of chains of global
+          // loads.  The stage holds no columns afterwards.
+          static_assert(sizeof(Job) <= sizeof(uint32_t) * kWarpStage, "Job must fit the stage");
+          const uint4 *src = reinterpret_cast<const uint4 *>(&J);
+          uint4 *dst = reinterpret_cast<uint4 *>(stage);
+          for (int i = lane; i < (int)(sizeof(Job) / 16); i += 32) dst[i] = __ldcg(src + i);
+          __syncwarp();
+          st_job = -1;
+          cs = -1;
+          const Job &F = *reinterpret_cast<const Job *>(stage);
           Winner wn;
-          if (!s_ml)
-            wn = winner_from_index(J, *reinterpret_cast<volatile unsigned long long *>(&J.best),
-                                   s_prob != 0);
-          else
-            wn = winner_ml(J);
-          finish_shot(b, *cdp, J, J.shot, wn, J.ebits, s_delta[warp]);
+          if (!s_ml) wn = winner_from_index(F, F.best, s_prob != 0);
+          else wn = winner_ml(F);
+          finish_shot(b, *cdp, F, F.shot, wn, F.ebits, s_delta[warp]);
+          __syncwarp();
         }
       }
     }

@@ -292,10 +292,16 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
   WarpArea &A = areas[wib];
-  const int gw = blockIdx.x * kTriageWarps + wib;
-  const int nwarps = gridDim.x * kTriageWarps;
 
-  for (int slot = gw; slot < b.num_shots; slot += nwarps) {
+  // Shots are drawn one at a time from a batch-wide counter, so a warp that
+  // drew cheap shots keeps drawing while another works through an expensive
+  // one.  The next draw is issued at the top of each shot and read at its end.
+  unsigned long long nxt = 0;
+  if (lane == 0) nxt = atomicAdd(&b.counters[3], 1ull);
+  for (int slot = __shfl_sync(kFull, (int)nxt, 0); slot < b.num_shots;
+       slot = __shfl_sync(kFull, (int)nxt, 0)) {
+    if (lane == 0) nxt = atomicAdd(&b.counters[3], 1ull);
+    const unsigned long long t_start = global_ns();
     const int shot = b.shot_map ? b.shot_map[slot] : slot;
     const int ci = b.shot_code ? b.shot_code[shot] : 0;
     const DevCode &cd = b.codes[ci];
@@ -307,7 +313,7 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
     int original_weight = 0;
     if (cd.input_kind == kInErrors) {
       original_weight = pack_ballots(rec, cd.m, A.eb);
-      prefetch_next_record(b, slot + nwarps);
+      prefetch_next_record(b, __shfl_sync(kFull, (int)nxt, 0));
       __syncwarp();
       // s = XOR of the columns of the supplied error (grand_decoder.cu:476-486)
       for (int q = 0; q < cd.mw; ++q) {
@@ -323,7 +329,7 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
       if (cd.family == kDem)
         pack_ballots(b.in_log ? b.in_log + (size_t)shot * cd.n_logicos : rec + cd.R, cd.n_logicos,
                      A.eb);
-      prefetch_next_record(b, slot + nwarps);
+      prefetch_next_record(b, __shfl_sync(kFull, (int)nxt, 0));
       __syncwarp();
       s_lane = lane < cd.nw ? A.sw[lane] : 0u;
     }
@@ -389,6 +395,8 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
       J.original_weight = original_weight;
       J.best = kNone;
       J.tiles_done = 0;
+      J.t_start = t_start;
+      J.t_counts = global_ns();
     }
 
     // ---- iterations in upstream order; the first one over the light budget
