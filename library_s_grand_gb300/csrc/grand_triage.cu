@@ -221,6 +221,84 @@ __device__ __forceinline__ void prefetch_next_record(const DevBatch &b, int slot
 }
 
 // ---------------------------------------------------------------------------
+// Small active sets: every subset as a bit mask.
+// ---------------------------------------------------------------------------
+constexpr int kSmallTam = 12;  // iterations with tam <= 12 take this path
+
+// All 2^tam subsets of a small active set in one pass.  Lane l walks the masks
+// gray(g) = g ^ (g >> 1) for g in its own contiguous block, so each step flips
+// one column: one shared-memory column load and NW XORs, with no unranking and
+// no per-weight tiles.  A mask of weight w that the iteration searches (bit w
+// of wmask) and whose columns XOR to the syndrome is a match; its global index
+// is the base of its weight block plus its lexicographic rank.  Since blocks
+// are laid out in search order, the lowest matching index over the warp is the
+// candidate the block-by-block search finds first.
+template <int NW>
+__device__ unsigned long long small_iteration(const uint32_t *cols, const uint32_t *sw, int tam,
+                                              const unsigned long long (&wbase)[kMaxW + 1],
+                                              unsigned wmask, const unsigned long long *t) {
+  constexpr int nwp = Words<NW>::nwp;
+  const int lane = threadIdx.x & 31;
+  const int nm = 1 << tam;
+  const int per = (nm + 31) >> 5;
+  const int g0 = lane * per;
+  const int g1 = g0 + per < nm ? g0 + per : nm;
+  unsigned long long best = kNone;
+  if (g0 < g1) {
+    unsigned mask = (unsigned)(g0 ^ (g0 >> 1));
+    uint32_t T[NW];  // syndrome XOR the mask's columns: zero on a match
+#pragma unroll
+    for (int i = 0; i < NW; ++i) T[i] = sw[i];
+    for (unsigned mm = mask; mm; mm &= mm - 1u) {
+      uint32_t a[NW];
+      load_words<NW>(cols + (__ffs(mm) - 1) * nwp, a);
+#pragma unroll
+      for (int i = 0; i < NW; ++i) T[i] ^= a[i];
+    }
+    for (int g = g0;;) {
+      uint32_t z = T[0];
+#pragma unroll
+      for (int i = 1; i < NW; ++i) z |= T[i];
+      const int w = __popc(mask);
+      if (z == 0u && ((wmask >> w) & 1u)) {
+        int x[5] = {0, 0, 0, 0, 0};
+        int k = 0, j = 0;
+        for (unsigned mm = mask; mm; mm &= mm - 1u) {
+          const int bit = __ffs(mm) - 1;
+          if (mm & (mm - 1u)) x[k++] = bit;
+          else j = bit;
+        }
+        const unsigned long long g_idx = wbase[w] + lex_rank(t, tam, w, x, w - 1, j);
+        if (g_idx < best) best = g_idx;
+      }
+      if (++g >= g1) break;
+      const int bit = __ffs(g) - 1;  // gray(g) ^ gray(g - 1) = 1 << ctz(g)
+      mask ^= 1u << bit;
+      uint32_t a[NW];
+      load_words<NW>(cols + bit * nwp, a);
+#pragma unroll
+      for (int i = 0; i < NW; ++i) T[i] ^= a[i];
+    }
+  }
+  return warp_min_u64(best);
+}
+
+__device__ unsigned long long small_dispatch(int nw, const uint32_t *cols, const uint32_t *sw,
+                                             int tam, const unsigned long long (&wbase)[kMaxW + 1],
+                                             unsigned wmask, const unsigned long long *t) {
+  switch (nw) {
+    case 1: return small_iteration<1>(cols, sw, tam, wbase, wmask, t);
+    case 2: return small_iteration<2>(cols, sw, tam, wbase, wmask, t);
+    case 3: return small_iteration<3>(cols, sw, tam, wbase, wmask, t);
+    case 4: return small_iteration<4>(cols, sw, tam, wbase, wmask, t);
+    case 5: return small_iteration<5>(cols, sw, tam, wbase, wmask, t);
+    case 6: return small_iteration<6>(cols, sw, tam, wbase, wmask, t);
+    case 7: return small_iteration<7>(cols, sw, tam, wbase, wmask, t);
+    default: return small_iteration<8>(cols, sw, tam, wbase, wmask, t);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Kernel 1: triage + light search.
 // ---------------------------------------------------------------------------
 __device__ void light_search(const DevBatch &b, const DevCode &cd, Job &J, WarpArea &A, int ii,
@@ -244,6 +322,21 @@ __device__ void light_search(const DevBatch &b, const DevCode &cd, Job &J, WarpA
   }
   __syncwarp();
   if (!ml) {
+    if (I.tam <= kSmallTam && cd.nw <= 8) {
+      // weight -> base of the block that searches it first (a later listing of
+      // the same weight never matches first)
+      unsigned long long wb[kMaxW + 1] = {0, 0, 0, 0, 0, 0, 0};
+      unsigned wm = 0;
+      for (int s = I.seg_lo; s < I.seg_hi; ++s) {
+        const Seg &S = J.seg[s];
+        if (S.dup) continue;
+        wb[S.w] = S.base;
+        wm |= 1u << S.w;
+      }
+      const unsigned long long g = small_dispatch(cd.nw, A.cols, A.sw, I.tam, wb, wm, b.ncr);
+      if (g != kNone) wn = winner_from_index(J, g, cd.variant == kProb);
+      return;
+    }
     for (int s = I.seg_lo; s < I.seg_hi && !wn.found; ++s) {
       const Seg &S = J.seg[s];
       if (S.dup) continue;
