@@ -223,7 +223,7 @@ __device__ __forceinline__ void prefetch_next_record(const DevBatch &b, int slot
 // ---------------------------------------------------------------------------
 // Small active sets: every subset as a bit mask.
 // ---------------------------------------------------------------------------
-constexpr int kSmallTam = 12;  // iterations with tam <= 12 take this path
+constexpr int kSmallTam = 14;  // iterations with tam <= 14 take this path
 
 // All 2^tam subsets of a small active set in one pass.  Lane l walks the masks
 // gray(g) = g ^ (g >> 1) for g in its own contiguous block, so each step flips
@@ -281,6 +281,89 @@ __device__ unsigned long long small_iteration(const uint32_t *cols, const uint32
     }
   }
   return warp_min_u64(best);
+}
+
+// The ML form: every matching mask's cost is its LLRs summed in ascending
+// position order (the order the block-by-block search adds them), and each
+// weight keeps the lowest {cost key, lexicographic rank}; O[w], R[w] return the
+// warp's minima per weight (0xffffffff / kNone: no match of weight w).
+template <int NW>
+__device__ void small_iteration_ml(const uint32_t *cols, const float *llr, const uint32_t *sw,
+                                   int tam, unsigned wmask, const unsigned long long *t,
+                                   uint32_t (&O)[kMaxW + 1], unsigned long long (&R)[kMaxW + 1]) {
+  constexpr int nwp = Words<NW>::nwp;
+  const int lane = threadIdx.x & 31;
+  const int nm = 1 << tam;
+  const int per = (nm + 31) >> 5;
+  const int g0 = lane * per;
+  const int g1 = g0 + per < nm ? g0 + per : nm;
+#pragma unroll
+  for (int q = 0; q <= kMaxW; ++q) {
+    O[q] = 0xffffffffu;
+    R[q] = kNone;
+  }
+  if (g0 < g1) {
+    unsigned mask = (unsigned)(g0 ^ (g0 >> 1));
+    uint32_t T[NW];
+#pragma unroll
+    for (int i = 0; i < NW; ++i) T[i] = sw[i];
+    for (unsigned mm = mask; mm; mm &= mm - 1u) {
+      uint32_t a[NW];
+      load_words<NW>(cols + (__ffs(mm) - 1) * nwp, a);
+#pragma unroll
+      for (int i = 0; i < NW; ++i) T[i] ^= a[i];
+    }
+    for (int g = g0;;) {
+      uint32_t z = T[0];
+#pragma unroll
+      for (int i = 1; i < NW; ++i) z |= T[i];
+      const int w = __popc(mask);
+      if (z == 0u && ((wmask >> w) & 1u)) {
+        int x[5] = {0, 0, 0, 0, 0};
+        int k = 0, j = 0;
+        float pc = 0.0f;
+        for (unsigned mm = mask; mm; mm &= mm - 1u) {
+          const int bit = __ffs(mm) - 1;
+          pc = __fadd_rn(pc, llr[bit]);
+          if (mm & (mm - 1u)) x[k++] = bit;
+          else j = bit;
+        }
+        const uint32_t o = cost_key(pc);
+        const unsigned long long r = lex_rank(t, tam, w, x, w - 1, j);
+#pragma unroll
+        for (int q = 1; q <= kMaxW; ++q)
+          if (q == w && (o < O[q] || (o == O[q] && r < R[q]))) {
+            O[q] = o;
+            R[q] = r;
+          }
+      }
+      if (++g >= g1) break;
+      const int bit = __ffs(g) - 1;
+      mask ^= 1u << bit;
+      uint32_t a[NW];
+      load_words<NW>(cols + bit * nwp, a);
+#pragma unroll
+      for (int i = 0; i < NW; ++i) T[i] ^= a[i];
+    }
+  }
+#pragma unroll
+  for (int q = 1; q <= kMaxW; ++q) warp_min_key(O[q], R[q]);
+}
+
+__device__ void small_dispatch_ml(int nw, const uint32_t *cols, const float *llr,
+                                  const uint32_t *sw, int tam, unsigned wmask,
+                                  const unsigned long long *t, uint32_t (&O)[kMaxW + 1],
+                                  unsigned long long (&R)[kMaxW + 1]) {
+  switch (nw) {
+    case 1: small_iteration_ml<1>(cols, llr, sw, tam, wmask, t, O, R); break;
+    case 2: small_iteration_ml<2>(cols, llr, sw, tam, wmask, t, O, R); break;
+    case 3: small_iteration_ml<3>(cols, llr, sw, tam, wmask, t, O, R); break;
+    case 4: small_iteration_ml<4>(cols, llr, sw, tam, wmask, t, O, R); break;
+    case 5: small_iteration_ml<5>(cols, llr, sw, tam, wmask, t, O, R); break;
+    case 6: small_iteration_ml<6>(cols, llr, sw, tam, wmask, t, O, R); break;
+    case 7: small_iteration_ml<7>(cols, llr, sw, tam, wmask, t, O, R); break;
+    default: small_iteration_ml<8>(cols, llr, sw, tam, wmask, t, O, R); break;
+  }
 }
 
 __device__ unsigned long long small_dispatch(int nw, const uint32_t *cols, const uint32_t *sw,
@@ -350,6 +433,14 @@ __device__ void light_search(const DevBatch &b, const DevCode &cd, Job &J, WarpA
     return;
   }
   // upstream search_cpu_ml (grand_decoder.cu:620-656), one weight at a time
+  const bool small = I.tam <= kSmallTam && cd.nw <= 8;
+  uint32_t SO[kMaxW + 1];
+  unsigned long long SR[kMaxW + 1];
+  if (small) {
+    unsigned wm = 0;
+    for (int s = I.seg_lo; s < I.seg_hi; ++s) wm |= 1u << J.seg[s].w;
+    small_dispatch_ml(cd.nw, A.cols, A.llr, A.sw, I.tam, wm, b.ncr, SO, SR);
+  }
   uint32_t bo = 0xffffffffu;
   unsigned long long br = kNone, proc = 0;
   int bseg = -1;
@@ -357,13 +448,26 @@ __device__ void light_search(const DevBatch &b, const DevCode &cd, Job &J, WarpA
     const Seg &S = J.seg[s];
     if (bseg >= 0 && I.prefix[S.w] >= key_cost(bo)) break;
     proc += S.count;
-    SegView sv{A.cols, A.llr, I.tam, S.w, S.K, cd.nwp, cd.nw, S.nprefix, S.base};
-    LaneBest lb;
-    lb.reset();
-    eval_segment<true>(cd, sv, S, b.ncr, A.sw, lb);
-    uint32_t o = lb.o;
-    unsigned long long r = lb.r;
-    warp_min_key(o, r);
+    uint32_t o;
+    unsigned long long r;
+    if (small) {
+      o = 0xffffffffu;
+      r = kNone;
+#pragma unroll
+      for (int q = 1; q <= kMaxW; ++q)
+        if (q == S.w) {
+          o = SO[q];
+          r = SR[q];
+        }
+    } else {
+      SegView sv{A.cols, A.llr, I.tam, S.w, S.K, cd.nwp, cd.nw, S.nprefix, S.base};
+      LaneBest lb;
+      lb.reset();
+      eval_segment<true>(cd, sv, S, b.ncr, A.sw, lb);
+      o = lb.o;
+      r = lb.r;
+      warp_min_key(o, r);
+    }
     if (o != 0xffffffffu && (bseg < 0 || o < bo)) {
       bo = o;
       br = r;
