@@ -353,7 +353,7 @@ def run_ours(args):
 STRESS_SHOTS = 192
 # DRAM bytes (read + write) of one search_kernel launch on the stress input, from an ncu
 # --set full capture of `bench.py --case stress` (48 shots), scaled to 192 shots.
-STRESS_TRAFFIC_PER_SHOT = (1.023488e6 + 21.76e3) / 48
+STRESS_TRAFFIC_PER_SHOT = (1.164288e6 + 133.888e3) / 48
 
 
 def stress_case(torch, lib, dev, n=STRESS_SHOTS):
