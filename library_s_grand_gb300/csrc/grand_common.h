@@ -11,13 +11,36 @@
 //   lcols  : m rows of L_dem packed into nlw words (DEM logical flips).
 //   llr    : m FP32 LLRs (ML variant).
 //   ncr    : C(n, k) for n <= GRAND_MAX_TAM, k <= 6, as uint64.
+//   hcol   : m 32-bit column sketches, hcol[c] = h(column c) with the GF(2)-linear
+//            hash h(v) = XOR of row_hash(r) over the set rows r of v.
 #pragma once
 
 #include <stdint.h>
 
 #include "grand_decoder.h"
 
+#ifdef __CUDACC__
+#define GRAND_HD __host__ __device__
+#else
+#define GRAND_HD
+#endif
+
 namespace grand {
+
+// Hash of one check row for the column sketches: MurmurHash3's 32-bit finalizer
+// (fmix32) of the row index.  The sketch of a vector is the XOR of its rows'
+// hashes, so it is linear over GF(2): the sketch of (syndrome XOR the columns of
+// a candidate) is the XOR of their sketches, and a candidate that matches has
+// sketch 0.  fmix32 is a bijection, so no two rows share a hash.
+GRAND_HD inline uint32_t row_hash(int r) {
+  uint32_t x = (uint32_t)r * 0x9E3779B9u + 0x7F4A7C15u;
+  x ^= x >> 16;
+  x *= 0x85EBCA6Bu;
+  x ^= x >> 13;
+  x *= 0xC2B2AE35u;
+  x ^= x >> 16;
+  return x;
+}
 
 constexpr int kMaxW = GRAND_MAX_W;        // searched weights 1..6
 constexpr int kMaxTam = GRAND_MAX_TAM;    // largest active set searched
@@ -62,6 +85,7 @@ struct DevCode {
   const int *pivrow;         // m: RREF row whose pivot is column c, or -1
   const uint32_t *lcols;     // m * nlw
   const float *llr;          // m
+  const uint32_t *hcol;      // m column sketches
 };
 
 // One searched weight block of one threshold iteration.
@@ -78,7 +102,7 @@ struct Seg {
   unsigned long long njt;    // tiles the search kernel runs for this block (0: none)
   const unsigned long long *cum; // run tiles: tiles before run c, c = 0..tam-1 (scratch)
   int K;                     // prefixes per lane in a tile
-  int runs;                  // 1: register-blocked run tiles (w >= 3, nw <= 8); 0: colex tiles
+  int runs;                  // 1: register-blocked run tiles (w >= 3); 0: colex tiles (w <= 2)
 };
 
 struct IterInfo {
@@ -92,6 +116,7 @@ struct IterInfo {
   unsigned long long phase_end[3]; // prob: cumulative full count through phase k
   float prefix[kMaxW + 1];   // ML: FP32 sums of the w smallest LLRs
   uint32_t *cols;            // tam * nwp staged columns (scratch)
+  uint32_t *hcols;           // tam staged column sketches (scratch)
   int *pos;                  // tam H-column indices (sorted by LLR for ML)
   float *llr;                // tam LLRs in the same order (ML)
 };
@@ -111,6 +136,7 @@ struct alignas(16) Job {
   unsigned long long tiles_done;
   int original_weight;
   int failed;                     // an active set exceeded the kernel limits
+  uint32_t hs;                    // sketch of the syndrome
   unsigned long long t_start;     // %globaltimer (ns) when the shot's triage began,
   unsigned long long t_counts;    //   and when its flagged-check counts were done
   uint32_t *ebits;                // mw words: supplied error (CSS) / truth logicals (DEM)

@@ -7,9 +7,10 @@
 // prefixes are dealt out in colex order, one prefix per lane, so the 32 lanes of
 // a warp usually share the same prefix maximum; the warp then walks j in
 // lockstep and every lane reads the same staged column (a shared-memory
-// broadcast).  Per candidate a lane does one XOR-OR chain over the column words
-// against T = s ^ (XOR of the prefix columns) and one min: T is updated
-// incrementally when the prefix advances, never recomputed per candidate.
+// broadcast).  Per candidate a lane does one XOR of 32-bit column sketches
+// against the sketch of s ^ (the prefix columns) and half a 3-way min: the
+// prefix sketch is updated incrementally when the prefix advances, never
+// recomputed per candidate, and a zero sketch is confirmed word by word.
 // Matches are mapped back to their lexicographic rank, so the reduction is an
 // exact minimum over the rank upstream would have reached first, whatever order
 // the tiles run in.
@@ -102,54 +103,12 @@ __device__ __forceinline__ float key_cost(uint32_t k) {
   return __uint_as_float(u);
 }
 
-template <int NW>
-struct Words {
-  static constexpr int nwp = NW <= 2 ? NW : (NW <= 4 ? 4 : 8);
-};
-
-// Column load + mismatch word for compile-time word counts (NW = 1..8); NW = 0
-// is the runtime-width fallback for R > 256.
-template <int NW>
-__device__ __forceinline__ uint32_t mismatch(const uint32_t *col, const uint32_t *T, int nw) {
-  if constexpr (NW == 1) {
-    return col[0] ^ T[0];
-  } else if constexpr (NW == 2) {
-    uint2 a = *reinterpret_cast<const uint2 *>(col);
-    return (a.x ^ T[0]) | (a.y ^ T[1]);
-  } else if constexpr (NW == 3 || NW == 4) {
-    uint4 a = *reinterpret_cast<const uint4 *>(col);
-    uint32_t z = (a.x ^ T[0]) | (a.y ^ T[1]) | (a.z ^ T[2]);
-    if constexpr (NW == 4) z |= a.w ^ T[3];
-    return z;
-  } else if constexpr (NW >= 5 && NW <= 8) {
-    uint4 a = *reinterpret_cast<const uint4 *>(col);
-    uint4 b = *reinterpret_cast<const uint4 *>(col + 4);
-    uint32_t z = (a.x ^ T[0]) | (a.y ^ T[1]) | (a.z ^ T[2]) | (a.w ^ T[3]) | (b.x ^ T[4]);
-    if constexpr (NW >= 6) z |= b.y ^ T[5];
-    if constexpr (NW >= 7) z |= b.z ^ T[6];
-    if constexpr (NW >= 8) z |= b.w ^ T[7];
-    return z;
-  } else {
-    uint32_t z = 0;
-    for (int i = 0; i < nw; ++i) z |= col[i] ^ T[i];
-    return z;
-  }
-}
-
-template <int NW>
-__device__ __forceinline__ void xor_col(uint32_t *T, const uint32_t *col, int nw) {
-  if constexpr (NW >= 1) {
-#pragma unroll
-    for (int i = 0; i < NW; ++i) T[i] ^= col[i];
-  } else {
-    for (int i = 0; i < nw; ++i) T[i] ^= col[i];
-  }
-}
-
 // What one tile evaluation needs to know about its weight block.
 struct SegView {
-  const uint32_t *cols;   // tam x nwp staged active columns
+  const uint32_t *hcols;  // tam column sketches of the active columns (staged)
+  const uint32_t *cols;   // tam x nwp active columns (exact test of sketch hits)
   const float *llr;       // tam LLRs in the same order (ML)
+  uint32_t hs;            // sketch of the syndrome
   int tam, w, K, nwp, nw;
   unsigned long long nprefix;
   unsigned long long base;  // global index of rank 0 (first-hit)
@@ -162,31 +121,77 @@ struct LaneBest {
   __device__ __forceinline__ void reset() { g = kNone; o = 0xffffffffu; r = kNone; }
 };
 
-// Evaluate one tile: lane l takes the K colex prefixes tile*32K + l*K + [0, K).
-template <int NW, bool ML>
+// Exact test of a sketch hit: the syndrome XOR the columns of prefix x[0..k-1]
+// and of j is zero in every word.
+__device__ __forceinline__ bool exact_match(const SegView &sv, const uint32_t *sw,
+                                            const int (&x)[5], int k, int j) {
+  for (int i = 0; i < sv.nw; ++i) {
+    uint32_t z = sw[i] ^ sv.cols[(size_t)j * sv.nwp + i];
+#pragma unroll
+    for (int e = 0; e < 5; ++e)
+      if (e < k) z ^= sv.cols[(size_t)x[e] * sv.nwp + i];
+    if (z != 0u) return false;
+  }
+  return true;
+}
+
+// A verified match: its global index (first-hit) or {cost key, rank} (ML) into
+// the lane's best.  ML costs add the LLRs in ascending position order.
+template <bool ML>
+__device__ __forceinline__ void record_match(const SegView &sv, const unsigned long long *t,
+                                             const int (&x)[5], int k, int j, LaneBest &lb) {
+  const unsigned long long r = lex_rank(t, sv.tam, sv.w, x, k, j);
+  if constexpr (!ML) {
+    const unsigned long long g = sv.base + r;
+    if (g < lb.g) lb.g = g;
+  } else {
+    float c = 0.0f;
+#pragma unroll
+    for (int e = 0; e < 5; ++e)
+      if (e < k) c = __fadd_rn(c, sv.llr[x[e]]);
+    c = __fadd_rn(c, sv.llr[j]);
+    const uint32_t o = cost_key(c);
+    if (o < lb.o || (o == lb.o && r < lb.r)) {
+      lb.o = o;
+      lb.r = r;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Sketch filter.
+//
+// A candidate matches when s ^ col(p_1) ^ ... ^ col(p_w) = 0 over all ceil(R/32)
+// words.  The scans below test a 32-bit linear sketch of that vector instead:
+// h(s) ^ h(col p_1) ^ ... ^ h(col p_w), which is 0 for every match (h is linear
+// and h(0) = 0) and, for a non-match, 0 only when the residual vector happens to
+// lie in the kernel of h.  A zero sketch is then tested word by word
+// (exact_match), so the result is exactly the word-by-word search's; the filter
+// only decides how much work a non-match costs: one XOR and half a 3-way minimum
+// per candidate, whatever the number of check rows.
+// ---------------------------------------------------------------------------
+
+// Evaluate one colex tile: lane l takes the K colex prefixes tile*32K + l*K + [0, K).
+template <bool ML>
 __device__ __forceinline__ void eval_tile(const SegView &sv, const unsigned long long *t,
-                                       const uint32_t *sw, unsigned long long tile, LaneBest &lb) {
-  constexpr int NWA = NW ? NW : 32;
+                                          const uint32_t *sw, unsigned long long tile,
+                                          LaneBest &lb) {
   const int lane = threadIdx.x & 31;
   const int k = sv.w - 1;
   const int tam = sv.tam;
-  const int nwp = NW ? Words<NW>::nwp : sv.nwp;
-  const int nw = NW ? NW : sv.nw;
-  const uint32_t *cols = sv.cols;
+  const uint32_t *hc = sv.hcols;
 
   unsigned long long q = tile * (32ull * (unsigned long long)sv.K) + (unsigned long long)lane * sv.K;
   bool valid = q < sv.nprefix;
   int x[5] = {0, 0, 0, 0, 0};
-  uint32_t T[NWA];
-#pragma unroll
-  for (int i = 0; i < NWA; ++i) T[i] = (i < nw) ? sw[i] : 0u;
+  uint32_t h = sv.hs;
   int clast = -1;
   if (valid && k > 0) {
     colex_unrank(t, q, k, tam - 2, x);
 #pragma unroll
     for (int i = 0; i < 5; ++i)
       if (i < k) {
-        xor_col<NW>(T, cols + (size_t)x[i] * nwp, nw);
+        h ^= hc[x[i]];
         clast = x[i];
       }
   }
@@ -200,34 +205,19 @@ __device__ __forceinline__ void eval_tile(const SegView &sv, const unsigned long
     int j = lo;
     const int ahi = hi < tam - 1 ? hi : tam - 1;
     for (; j <= ahi; ++j) {
-      uint32_t z = mismatch<NW>(cols + (size_t)j * nwp, T, nw);
+      const uint32_t z = h ^ hc[j];
       if (j > cl) acc = min(acc, z);
     }
     if (j < hi + 1) j = hi + 1;
 #pragma unroll 4
-    for (; j < tam; ++j) acc = min(acc, mismatch<NW>(cols + (size_t)j * nwp, T, nw));
+    for (; j < tam; ++j) acc = min(acc, h ^ hc[j]);
 
     if (v && acc == 0u) {
-      // A match exists for this prefix: locate it (rare path).
+      // A zero sketch for this prefix: test those candidates word by word (rare).
       for (int jj = cl + 1; jj < tam; ++jj) {
-        if (mismatch<NW>(cols + (size_t)jj * nwp, T, nw) != 0u) continue;
-        unsigned long long r = lex_rank(t, tam, sv.w, x, k, jj);
-        if constexpr (!ML) {
-          unsigned long long g = sv.base + r;
-          if (g < lb.g) lb.g = g;
-          break;
-        } else {
-          float c = 0.0f;
-#pragma unroll
-          for (int i = 0; i < 5; ++i)
-            if (i < k) c = __fadd_rn(c, sv.llr[x[i]]);
-          c = __fadd_rn(c, sv.llr[jj]);
-          uint32_t o = cost_key(c);
-          if (o < lb.o || (o == lb.o && r < lb.r)) {
-            lb.o = o;
-            lb.r = r;
-          }
-        }
+        if ((h ^ hc[jj]) != 0u || !exact_match(sv, sw, x, k, jj)) continue;
+        record_match<ML>(sv, t, x, k, jj, lb);
+        if constexpr (!ML) break;  // ranks grow with the last index
       }
     }
 
@@ -248,11 +238,10 @@ __device__ __forceinline__ void eval_tile(const SegView &sv, const unsigned long
 #pragma unroll
         for (int i = 0; i < 5; ++i) {
           if (i < k && i <= adv) {
-            int old = x[i];
-            int nv = (i == adv) ? old + 1 : i;
+            const int old = x[i];
+            const int nv = (i == adv) ? old + 1 : i;
             if (nv != old) {
-              xor_col<NW>(T, cols + (size_t)old * nwp, nw);
-              xor_col<NW>(T, cols + (size_t)nv * nwp, nw);
+              h ^= hc[old] ^ hc[nv];
               x[i] = nv;
             }
           }
@@ -266,48 +255,15 @@ __device__ __forceinline__ void eval_tile(const SegView &sv, const unsigned long
 }
 
 // ---------------------------------------------------------------------------
-// Register-blocked tiles for weights >= 3 (NW = 1..8).
+// Register-blocked run tiles for weights >= 3.
 //
 // The (w-1)-prefixes whose largest element is c form one contiguous colex run
 // of C(c, w-2) prefixes (their other w-2 elements are any subset of [0, c)).  A
 // run tile gives each lane KK consecutive prefixes of one run, so every prefix
 // in the warp has the same largest element: the warp walks j = c+1 .. tam-1 in
-// lockstep with no masking, loads column j once (shared-memory broadcast) and
-// compares it against the KK T vectors each lane keeps in registers.  Per
-// candidate that is NW XOR-OR word operations and half a 3-way minimum.
+// lockstep with no masking, loads sketch j once (shared-memory broadcast) and
+// XORs it into the KK prefix sketches each lane keeps in registers.
 // ---------------------------------------------------------------------------
-template <int NW>
-__device__ __forceinline__ void load_words(const uint32_t *col, uint32_t (&a)[NW]) {
-  if constexpr (NW == 1) {
-    a[0] = col[0];
-  } else if constexpr (NW == 2) {
-    uint2 v = *reinterpret_cast<const uint2 *>(col);
-    a[0] = v.x; a[1] = v.y;
-  } else if constexpr (NW <= 4) {
-    uint4 v = *reinterpret_cast<const uint4 *>(col);
-    a[0] = v.x; a[1] = v.y; a[2] = v.z;
-    if constexpr (NW == 4) a[3] = v.w;
-  } else {
-    uint4 v = *reinterpret_cast<const uint4 *>(col);
-    uint4 u = *reinterpret_cast<const uint4 *>(col + 4);
-    a[0] = v.x; a[1] = v.y; a[2] = v.z; a[3] = v.w; a[4] = u.x;
-    if constexpr (NW >= 6) a[5] = u.y;
-    if constexpr (NW >= 7) a[6] = u.z;
-    if constexpr (NW >= 8) a[7] = u.w;
-  }
-}
-
-// z = OR_i (a[i] ^ T[i]): one lop3 per word.  LUT 0x3C is a ^ b; LUT 0xBE is
-// (a ^ b) | c, so each further word folds its XOR and the running OR together.
-template <int NW>
-__device__ __forceinline__ uint32_t diff_words(const uint32_t (&a)[NW], const uint32_t (&T)[NW]) {
-  uint32_t z;
-  asm("lop3.b32 %0, %1, %2, 0, 0x3C;" : "=r"(z) : "r"(a[0]), "r"(T[0]));
-#pragma unroll
-  for (int i = 1; i < NW; ++i)
-    asm("lop3.b32 %0, %1, %2, %3, 0xBE;" : "=r"(z) : "r"(a[i]), "r"(T[i]), "r"(z));
-  return z;
-}
 
 // Colex successor of an ascending kk-subset y of [0, c); returns the highest
 // changed position (elements 0..adv changed), -1 when exhausted.
@@ -366,51 +322,31 @@ __device__ __forceinline__ int sub_next(int (&y)[5], int kk, int c) {
   return colex_next(y, kk, c);
 }
 
-template <int NW>
-__device__ __forceinline__ void prefix_T(const uint32_t *cols, int nwp, const uint32_t (&base)[NW],
-                                         const int (&y)[5], int kk, uint32_t (&T)[NW]) {
-#pragma unroll
-  for (int i = 0; i < NW; ++i) T[i] = base[i];
-#pragma unroll
-  for (int e = 0; e < 5; ++e)
-    if (e < kk) {
-      uint32_t a[NW];
-      load_words<NW>(cols + (size_t)y[e] * nwp, a);
-#pragma unroll
-      for (int i = 0; i < NW; ++i) T[i] ^= a[i];
-    }
-}
-
 // One run tile: run c, lane l takes prefixes r0 + l*KK + [0, KK) of the run.
-template <int NW, int KK, bool ML>
+template <int KK, bool ML>
 __device__ __forceinline__ void eval_run_tile(const SegView &sv, const unsigned long long *t,
                                               const uint32_t *sw, int c, unsigned long long r0,
                                               LaneBest &lb) {
-  constexpr int nwp = Words<NW>::nwp;
   const int lane = threadIdx.x & 31;
   const int k = sv.w - 1;   // prefix length (>= 2)
   const int kk = k - 1;     // elements below c (>= 1)
   const int tam = sv.tam;
-  const uint32_t *cols = sv.cols;
+  const uint32_t *hc = sv.hcols;
   const unsigned long long run = ncr(t, c, kk);
   const unsigned long long r = r0 + (unsigned long long)lane * KK;
   const int v = r >= run ? 0 : (int)((run - r) < (unsigned long long)KK ? (run - r) : KK);
 
-  uint32_t base[NW];
-  {
-    uint32_t a[NW];
-    load_words<NW>(cols + (size_t)c * nwp, a);
-#pragma unroll
-    for (int i = 0; i < NW; ++i) base[i] = sw[i] ^ a[i];
-  }
+  const uint32_t hb = sv.hs ^ hc[c];
   int y[5] = {0, 1, 2, 3, 4};
   if (v > 0) sub_unrank(t, r, kk, c, y);
-  uint32_t T[KK][NW];
-  prefix_T<NW>(cols, nwp, base, y, kk, T[0]);
+  uint32_t H[KK];  // sketches of s ^ (the lane's prefixes)
+  H[0] = hb;
+#pragma unroll
+  for (int e = 0; e < 5; ++e)
+    if (e < kk) H[0] ^= hc[y[e]];
 #pragma unroll
   for (int s = 1; s < KK; ++s) {
-#pragma unroll
-    for (int i = 0; i < NW; ++i) T[s][i] = T[s - 1][i];
+    H[s] = H[s - 1];
     if (s < v) {
       int old[5];
 #pragma unroll
@@ -418,67 +354,41 @@ __device__ __forceinline__ void eval_run_tile(const SegView &sv, const unsigned 
       const int adv = sub_next(y, kk, c);
 #pragma unroll
       for (int e = 0; e < 5; ++e)
-        if (e < kk && e <= adv && old[e] != y[e]) {
-          uint32_t a[NW], b2[NW];
-          load_words<NW>(cols + (size_t)old[e] * nwp, a);
-          load_words<NW>(cols + (size_t)y[e] * nwp, b2);
-#pragma unroll
-          for (int i = 0; i < NW; ++i) T[s][i] ^= a[i] ^ b2[i];
-        }
-    } else {
-#pragma unroll
-      for (int i = 0; i < NW; ++i) T[s][i] = T[0][i];
+        if (e < kk && e <= adv && old[e] != y[e]) H[s] ^= hc[old[e]] ^ hc[y[e]];
     }
   }
 
   uint32_t acc = 0xffffffffu;
-#pragma unroll 2
+#pragma unroll 4
   for (int j = c + 1; j < tam; ++j) {
-    uint32_t a[NW];
-    load_words<NW>(cols + (size_t)j * nwp, a);
+    const uint32_t hj = hc[j];
     if constexpr (KK % 2 == 0) {
 #pragma unroll
-      for (int s = 0; s < KK; s += 2)
-        acc = __vimin3_u32(acc, diff_words<NW>(a, T[s]), diff_words<NW>(a, T[s + 1]));
+      for (int s = 0; s < KK; s += 2) acc = __vimin3_u32(acc, H[s] ^ hj, H[s + 1] ^ hj);
     } else {
 #pragma unroll
-      for (int s = 0; s < KK; ++s) acc = min(acc, diff_words<NW>(a, T[s]));
+      for (int s = 0; s < KK; ++s) acc = min(acc, H[s] ^ hj);
     }
   }
 
   if (v > 0 && acc == 0u) {
-    // At least one of this lane's prefixes has a match: find them all (rare).
+    // A zero sketch among this lane's prefixes: test those candidates word by
+    // word (rare; lanes without valid prefixes only repeat prefix 0's sketch).
     int yy[5] = {0, 1, 2, 3, 4};
     sub_unrank(t, r, kk, c, yy);
     for (int s = 0; s < v; ++s) {
       if (s > 0) sub_next(yy, kk, c);
-      uint32_t Ts[NW];
-      prefix_T<NW>(cols, nwp, base, yy, kk, Ts);
+      uint32_t hp = hb;
       int x[5];
 #pragma unroll
-      for (int e = 0; e < 5; ++e) x[e] = (e < kk) ? yy[e] : (e == kk ? c : 0);
-      float pc = 0.0f;
-      if constexpr (ML) {
-#pragma unroll
-        for (int e = 0; e < 5; ++e)
-          if (e < k) pc = __fadd_rn(pc, sv.llr[x[e]]);
+      for (int e = 0; e < 5; ++e) {
+        if (e < kk) hp ^= hc[yy[e]];
+        x[e] = (e < kk) ? yy[e] : (e == kk ? c : 0);
       }
       for (int j = c + 1; j < tam; ++j) {
-        uint32_t a[NW];
-        load_words<NW>(cols + (size_t)j * nwp, a);
-        if (diff_words<NW>(a, Ts) != 0u) continue;
-        const unsigned long long rk = lex_rank(t, tam, sv.w, x, k, j);
-        if constexpr (!ML) {
-          const unsigned long long g = sv.base + rk;
-          if (g < lb.g) lb.g = g;
-          break;
-        } else {
-          const uint32_t o = cost_key(__fadd_rn(pc, sv.llr[j]));
-          if (o < lb.o || (o == lb.o && rk < lb.r)) {
-            lb.o = o;
-            lb.r = rk;
-          }
-        }
+        if ((hp ^ hc[j]) != 0u || !exact_match(sv, sw, x, k, j)) continue;
+        record_match<ML>(sv, t, x, k, j, lb);
+        if constexpr (!ML) break;  // ranks grow with the last index
       }
     }
   }

@@ -63,6 +63,7 @@ CodeTables::~CodeTables() {
   cudaFree(rref);
   cudaFree(pivrow);
   cudaFree(lcols);
+  cudaFree(hcol);
 }
 
 Workspace::~Workspace() {
@@ -264,8 +265,15 @@ std::shared_ptr<CodeTables> Context::tables(int family, const int *H, const int 
   t->regular = 1;
   for (int c = 1; c < m; ++c)
     if (colw[c] != colw[0]) { t->regular = 0; break; }
+  std::vector<uint32_t> hcol(m, 0u);
+  for (int r = 0; r < n; ++r) {
+    const uint32_t hr = row_hash(r);
+    for (int c = 0; c < m; ++c)
+      if (H[(size_t)r * m + c] != 0) hcol[c] ^= hr;
+  }
   cudaError_t e = upload(&t->cols, cols);
   if (e == cudaSuccess) e = upload(&t->colw, colw);
+  if (e == cudaSuccess) e = upload(&t->hcol, hcol);
   if (e == cudaSuccess && family == kCss) {
     std::vector<uint32_t> rows((size_t)n * t->mw, 0u);
     for (int r = 0; r < n; ++r)
@@ -291,7 +299,7 @@ std::shared_ptr<CodeTables> Context::tables(int family, const int *H, const int 
     *err = GRAND_ERR_CUDA;
     return nullptr;
   }
-  t->bytes = cols.size() * 4 + colw.size() * 4 + key.size() * 4;
+  t->bytes = cols.size() * 4 + colw.size() * 4 + hcol.size() * 4 + key.size() * 4;
   t->key.swap(key);
   std::lock_guard<std::mutex> lk(mu_);
   cache_.push_back(t);
@@ -336,6 +344,7 @@ DevCode make_devcode(const CodeTables &t, const CallParams &p) {
   d.pivrow = t.pivrow;
   d.lcols = t.lcols;
   d.llr = p.d_llr;
+  d.hcol = t.hcol;
   return d;
 }
 

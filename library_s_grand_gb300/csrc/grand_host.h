@@ -32,6 +32,7 @@ struct CodeTables {
   uint32_t *rref = nullptr;
   int *pivrow = nullptr;
   uint32_t *lcols = nullptr;
+  uint32_t *hcol = nullptr;  // column sketches (row_hash XOR over each column's rows)
   std::vector<int> key;  // exact content the tables were built from
   size_t bytes = 0;
   ~CodeTables();

@@ -1,6 +1,5 @@
 // grand_kernels.cuh -- what the triage and search kernels share: launch
-// constants, the per-shot result writer, the first-hit winner lookup and the
-// evaluation dispatch on the column word count.  The two kernels live in their
+// constants, the per-shot result writer and the first-hit winner lookup.  The two kernels live in their
 // own translation units (grand_triage.cu, grand_search.cu) so they compile in
 // parallel.
 #pragma once
@@ -177,42 +176,6 @@ static __device__ Winner winner_from_index(const Job &J, unsigned long long g, b
     }
   }
   return wn;
-}
-
-// ---------------------------------------------------------------------------
-// Evaluation dispatch on the column word count.
-// ---------------------------------------------------------------------------
-template <bool ML>
-__device__ __forceinline__ void eval_dispatch(int nw, const SegView &sv,
-                                              const unsigned long long *t, const uint32_t *sw,
-                                              unsigned long long tile, LaneBest &lb) {
-  switch (nw) {
-    case 1: eval_tile<1, ML>(sv, t, sw, tile, lb); break;
-    case 2: eval_tile<2, ML>(sv, t, sw, tile, lb); break;
-    case 3: eval_tile<3, ML>(sv, t, sw, tile, lb); break;
-    case 4: eval_tile<4, ML>(sv, t, sw, tile, lb); break;
-    case 5: eval_tile<5, ML>(sv, t, sw, tile, lb); break;
-    case 6: eval_tile<6, ML>(sv, t, sw, tile, lb); break;
-    case 7: eval_tile<7, ML>(sv, t, sw, tile, lb); break;
-    case 8: eval_tile<8, ML>(sv, t, sw, tile, lb); break;
-    default: eval_tile<0, ML>(sv, t, sw, tile, lb); break;
-  }
-}
-
-template <bool ML, int KK>
-__device__ __forceinline__ void eval_run_dispatch(int nw, const SegView &sv,
-                                                  const unsigned long long *t, const uint32_t *sw,
-                                                  int c, unsigned long long r0, LaneBest &lb) {
-  switch (nw) {
-    case 1: eval_run_tile<1, KK, ML>(sv, t, sw, c, r0, lb); break;
-    case 2: eval_run_tile<2, KK, ML>(sv, t, sw, c, r0, lb); break;
-    case 3: eval_run_tile<3, KK, ML>(sv, t, sw, c, r0, lb); break;
-    case 4: eval_run_tile<4, KK, ML>(sv, t, sw, c, r0, lb); break;
-    case 5: eval_run_tile<5, KK, ML>(sv, t, sw, c, r0, lb); break;
-    case 6: eval_run_tile<6, KK, ML>(sv, t, sw, c, r0, lb); break;
-    case 7: eval_run_tile<7, KK, ML>(sv, t, sw, c, r0, lb); break;
-    default: eval_run_tile<8, KK, ML>(sv, t, sw, c, r0, lb); break;
-  }
 }
 
 }  // namespace grand

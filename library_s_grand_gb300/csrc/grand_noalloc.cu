@@ -35,7 +35,8 @@ constexpr size_t kOffNcr = 0;
 constexpr size_t kOffCode = align256(kOffNcr + sizeof(unsigned long long) * (kMaxTam + 1) * (kMaxW + 1));
 constexpr size_t kOffCols = align256(kOffCode + sizeof(DevCode));
 constexpr size_t kOffColw = align256(kOffCols + sizeof(uint32_t) * kNaMaxCols * 8);
-constexpr size_t kOffSmall = align256(kOffColw + sizeof(int) * kNaMaxCols);  // counters, +128: status
+constexpr size_t kOffHcol = align256(kOffColw + sizeof(int) * kNaMaxCols);
+constexpr size_t kOffSmall = align256(kOffHcol + sizeof(uint32_t) * kNaMaxCols);  // counters, +128: status
 constexpr size_t kOffDeferred = align256(kOffSmall + 256);
 constexpr size_t kOffJobs = align256(kOffDeferred + sizeof(int) * kNaChunk);
 constexpr size_t kOffArena = align256(kOffJobs + sizeof(Job) * kNaChunk);
@@ -64,19 +65,26 @@ __global__ void noalloc_ncr_kernel(unsigned long long *t) {
   }
 }
 
-// One thread per column: packed bits (LSB-first, nwp words) and the column weight.
-__global__ void noalloc_pack_kernel(const int *H, int n, int m, int nwp, uint32_t *cols, int *colw) {
+// One thread per column: packed bits (LSB-first, nwp words), the column weight
+// and the column sketch.
+__global__ void noalloc_pack_kernel(const int *H, int n, int m, int nwp, uint32_t *cols, int *colw,
+                                    uint32_t *hcol) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= m) return;
   uint32_t w[8] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
+  uint32_t h = 0u;
   int sum = 0;
   for (int r = 0; r < n; ++r) {
     const int v = H[(size_t)r * m + c];
     sum += v;
-    if (v != 0) w[r >> 5] |= 1u << (r & 31);
+    if (v != 0) {
+      w[r >> 5] |= 1u << (r & 31);
+      h ^= row_hash(r);
+    }
   }
   for (int i = 0; i < nwp; ++i) cols[(size_t)c * nwp + i] = w[i];
   colw[c] = sum;
+  hcol[c] = h;
 }
 
 // One block: maximum column weight and regularity, then the code descriptor.
@@ -185,6 +193,7 @@ extern "C" int grand_decode_cc_noalloc(const int *d_H, int n, int m, const int *
   const int nwp = nw <= 2 ? nw : (nw <= 4 ? 4 : 8);
   uint32_t *cols = reinterpret_cast<uint32_t *>(base + kOffCols);
   int *colw = reinterpret_cast<int *>(base + kOffColw);
+  uint32_t *hcol = reinterpret_cast<uint32_t *>(base + kOffHcol);
   DevCode *code = reinterpret_cast<DevCode *>(base + kOffCode);
 
   DevCode t;
@@ -205,8 +214,9 @@ extern "C" int grand_decode_cc_noalloc(const int *d_H, int n, int m, const int *
   t.rec_len = n;
   t.cols = cols;
   t.colw = colw;
+  t.hcol = hcol;
 
-  noalloc_pack_kernel<<<(m + 127) / 128, 128, 0, s>>>(d_H, n, m, nwp, cols, colw);
+  noalloc_pack_kernel<<<(m + 127) / 128, 128, 0, s>>>(d_H, n, m, nwp, cols, colw, hcol);
   noalloc_code_kernel<<<1, 256, 0, s>>>(t, colw, m, code);
   e = cudaGetLastError();
   // the status word starts at zero for every call; it then collects all chunks

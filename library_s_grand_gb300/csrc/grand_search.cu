@@ -109,7 +109,7 @@ __global__ void __launch_bounds__(kSearchThreads, 3) search_kernel(DevBatch b) {
   Job *Jp = nullptr;
   const DevCode *cdp = nullptr;
   SegView sv{};
-  int s_runs = 0, s_iter = 0, s_ml = 0, s_prob = 0, s_nw = 0;
+  int s_runs = 0, s_iter = 0, s_ml = 0, s_prob = 0;
   const unsigned long long *s_cum = nullptr;
 
   // Tiles are drawn kTilesPerFetch at a time when there are many per warp, one
@@ -163,18 +163,19 @@ __global__ void __launch_bounds__(kSearchThreads, 3) search_kernel(DevBatch b) {
         s_runs = S.runs;
         s_cum = S.cum;
         s_iter = S.iter;
-        s_nw = cdp->nw;
         s_ml = cdp->variant == kMl;
         s_prob = cdp->variant == kProb;
-        const bool staged = I.tam * cdp->nwp <= kWarpStage;
-        sv = SegView{staged ? stage : I.cols, I.llr, I.tam, S.w, S.K, cdp->nwp, cdp->nw,
-                     S.nprefix, S.base};
+        // the scans read only the column sketches: those are staged (the full
+        // columns are read from the Job's scratch for the rare exact tests)
+        const bool staged = I.tam <= kWarpStage;
+        sv = SegView{staged ? stage : I.hcols, I.cols, I.llr, J.hs, I.tam, S.w, S.K, cdp->nwp,
+                     cdp->nw, S.nprefix, S.base};
         if (st_job != cj || st_it != S.iter) {
           __syncwarp();
           if (staged) {
-            const uint4 *src = reinterpret_cast<const uint4 *>(I.cols);
+            const uint4 *src = reinterpret_cast<const uint4 *>(I.hcols);
             uint4 *dst = reinterpret_cast<uint4 *>(stage);
-            const int n4 = (I.tam * cdp->nwp + 3) / 4;
+            const int n4 = (I.tam + 3) / 4;
             for (int i = lane; i < n4; i += 32) dst[i] = src[i];
           }
           sw[lane] = J.sw[lane];
@@ -203,11 +204,11 @@ __global__ void __launch_bounds__(kSearchThreads, 3) search_kernel(DevBatch b) {
             cc_hi = cc_lo + run_tiles(b.ncr, clo, sv.w, kRunKK);
           }
           const unsigned long long r0 = (st - cc_lo) * (32ull * kRunKK);
-          if (s_ml) eval_run_dispatch<true, kRunKK>(s_nw, sv, b.ncr, sw, cc, r0, lb);
-          else eval_run_dispatch<false, kRunKK>(s_nw, sv, b.ncr, sw, cc, r0, lb);
+          if (s_ml) eval_run_tile<kRunKK, true>(sv, b.ncr, sw, cc, r0, lb);
+          else eval_run_tile<kRunKK, false>(sv, b.ncr, sw, cc, r0, lb);
         } else {
-          if (s_ml) eval_dispatch<true>(s_nw, sv, b.ncr, sw, st, lb);
-          else eval_dispatch<false>(s_nw, sv, b.ncr, sw, st, lb);
+          if (s_ml) eval_tile<true>(sv, b.ncr, sw, st, lb);
+          else eval_tile<false>(sv, b.ncr, sw, st, lb);
         }
         if (!s_ml) {
           const unsigned long long g = warp_min_u64(lb.g);

@@ -16,6 +16,7 @@ namespace grand {
 
 struct alignas(16) WarpArea {
   uint32_t cols[kLightWords];
+  uint32_t hcols[kLightTam];
   float llr[kLightTam];
   int pos[kLightTam];
   int tmp[kLightTam];
@@ -95,9 +96,9 @@ __device__ int plan_next(const DevCode &cd, const unsigned long long *t, const i
       S.count = ncr(t, tam, S.w);
       S.base = P.gbase + tot;
       S.nprefix = ncr(t, tam - 1, S.w - 1);
-      S.runs = (S.w >= 3 && cd.nw <= 8) ? 1 : 0;
+      S.runs = S.w >= 3 ? 1 : 0;
       S.cum = nullptr;
-      S.K = S.runs ? kRunKK : (S.w <= 2 ? 1 : tile_k);
+      S.K = S.runs ? kRunKK : tile_k;
       // run-tile counts are built by the warp when a Job is published
       S.ntiles = S.runs ? 0ull : (S.nprefix + 32ull * S.K - 1) / (32ull * S.K);
       tot += S.count;
@@ -118,10 +119,10 @@ __device__ int plan_next(const DevCode &cd, const unsigned long long *t, const i
 }
 
 // ---------------------------------------------------------------------------
-// Staging of one iteration's active set (positions, columns, LLRs).
+// Staging of one iteration's active set (positions, columns, sketches, LLRs).
 // ---------------------------------------------------------------------------
 __device__ void stage_iteration(const DevCode &cd, const uint32_t *am, int tam, int *pos,
-                                int *tmp, uint32_t *cols, float *llr) {
+                                int *tmp, uint32_t *cols, uint32_t *hcols, float *llr) {
   const int lane = threadIdx.x & 31;
   const bool ml = cd.variant == kMl;
   int *dst = ml ? tmp : pos;
@@ -153,6 +154,7 @@ __device__ void stage_iteration(const DevCode &cd, const uint32_t *am, int tam, 
     const int i = idx / nwp;
     cols[idx] = __ldg(cd.cols + (size_t)pos[i] * nwp + (idx - i * nwp));
   }
+  for (int i = lane; i < tam; i += 32) hcols[i] = __ldg(cd.hcol + pos[i]);
   if (ml)
     for (int i = lane; i < tam; i += 32) llr[i] = __ldg(cd.llr + pos[i]);
   __syncwarp();
@@ -167,11 +169,10 @@ __device__ void eval_segment(const DevCode &cd, const SegView &sv, const Seg &S,
     for (int c = S.w - 2; c <= sv.tam - 2; ++c) {
       const unsigned long long nt = run_tiles(t, c, S.w, kRunKKLight);
       for (unsigned long long q = 0; q < nt; ++q)
-        eval_run_dispatch<ML, kRunKKLight>(cd.nw, sv, t, sw, c, q * per, lb);
+        eval_run_tile<kRunKKLight, ML>(sv, t, sw, c, q * per, lb);
     }
   } else {
-    for (unsigned long long tile = 0; tile < S.ntiles; ++tile)
-      eval_dispatch<ML>(cd.nw, sv, t, sw, tile, lb);
+    for (unsigned long long tile = 0; tile < S.ntiles; ++tile) eval_tile<ML>(sv, t, sw, tile, lb);
   }
 }
 
@@ -225,78 +226,44 @@ __device__ __forceinline__ void prefetch_next_record(const DevBatch &b, int slot
 // ---------------------------------------------------------------------------
 constexpr int kSmallTam = 14;  // iterations with tam <= 14 take this path
 
-// All 2^tam subsets of a small active set in one pass.  Lane l walks the masks
-// gray(g) = g ^ (g >> 1) for g in its own contiguous block, so each step flips
-// one column: one shared-memory column load and NW XORs, with no unranking and
-// no per-weight tiles.  A mask of weight w that the iteration searches (bit w
-// of wmask) and whose columns XOR to the syndrome is a match; its global index
-// is the base of its weight block plus its lexicographic rank.  Since blocks
-// are laid out in search order, the lowest matching index over the warp is the
-// candidate the block-by-block search finds first.
-template <int NW>
-__device__ unsigned long long small_iteration(const uint32_t *cols, const uint32_t *sw, int tam,
-                                              const unsigned long long (&wbase)[kMaxW + 1],
-                                              unsigned wmask, const unsigned long long *t) {
-  constexpr int nwp = Words<NW>::nwp;
-  const int lane = threadIdx.x & 31;
-  const int nm = 1 << tam;
-  const int per = (nm + 31) >> 5;
-  const int g0 = lane * per;
-  const int g1 = g0 + per < nm ? g0 + per : nm;
-  unsigned long long best = kNone;
-  if (g0 < g1) {
-    unsigned mask = (unsigned)(g0 ^ (g0 >> 1));
-    uint32_t T[NW];  // syndrome XOR the mask's columns: zero on a match
-#pragma unroll
-    for (int i = 0; i < NW; ++i) T[i] = sw[i];
-    for (unsigned mm = mask; mm; mm &= mm - 1u) {
-      uint32_t a[NW];
-      load_words<NW>(cols + (__ffs(mm) - 1) * nwp, a);
-#pragma unroll
-      for (int i = 0; i < NW; ++i) T[i] ^= a[i];
-    }
-    for (int g = g0;;) {
-      uint32_t z = T[0];
-#pragma unroll
-      for (int i = 1; i < NW; ++i) z |= T[i];
-      const int w = __popc(mask);
-      if (z == 0u && ((wmask >> w) & 1u)) {
-        int x[5] = {0, 0, 0, 0, 0};
-        int k = 0, j = 0;
-        for (unsigned mm = mask; mm; mm &= mm - 1u) {
-          const int bit = __ffs(mm) - 1;
-          if (mm & (mm - 1u)) x[k++] = bit;
-          else j = bit;
-        }
-        const unsigned long long g_idx = wbase[w] + lex_rank(t, tam, w, x, w - 1, j);
-        if (g_idx < best) best = g_idx;
-      }
-      if (++g >= g1) break;
-      const int bit = __ffs(g) - 1;  // gray(g) ^ gray(g - 1) = 1 << ctz(g)
-      mask ^= 1u << bit;
-      uint32_t a[NW];
-      load_words<NW>(cols + bit * nwp, a);
-#pragma unroll
-      for (int i = 0; i < NW; ++i) T[i] ^= a[i];
-    }
+// Exact test of a mask whose sketch is zero: the syndrome XOR the mask's
+// columns is zero in every word.
+__device__ __forceinline__ bool mask_matches(const uint32_t *cols, int nwp, int nw,
+                                             const uint32_t *sw, unsigned mask) {
+  for (int i = 0; i < nw; ++i) {
+    uint32_t z = sw[i];
+    for (unsigned mm = mask; mm; mm &= mm - 1u) z ^= cols[(__ffs(mm) - 1) * nwp + i];
+    if (z != 0u) return false;
   }
-  return warp_min_u64(best);
+  return true;
 }
 
-// The ML form: every matching mask's cost is its LLRs summed in ascending
-// position order (the order the block-by-block search adds them), and each
-// weight keeps the lowest {cost key, lexicographic rank}; O[w], R[w] return the
-// warp's minima per weight (0xffffffff / kNone: no match of weight w).
-template <int NW>
-__device__ void small_iteration_ml(const uint32_t *cols, const float *llr, const uint32_t *sw,
-                                   int tam, unsigned wmask, const unsigned long long *t,
-                                   uint32_t (&O)[kMaxW + 1], unsigned long long (&R)[kMaxW + 1]) {
-  constexpr int nwp = Words<NW>::nwp;
+// All 2^tam subsets of a small active set in one pass.  Lane l walks the masks
+// gray(g) = g ^ (g >> 1) for g in its own contiguous block, so each step flips
+// one column: one shared-memory sketch load and one XOR, with no unranking and
+// no per-weight tiles.  A mask of weight w that the iteration searches (bit w of
+// wmask), whose sketch is zero and whose columns XOR to the syndrome word by
+// word, is a match.
+//   first-hit: its global index is the base of its weight block plus its
+//     lexicographic rank; blocks are laid out in search order, so the lowest
+//     index over the warp (best) is the candidate the block-by-block search
+//     finds first;
+//   ML: its cost is its LLRs summed in ascending position order (the order the
+//     block-by-block search adds them), and each weight keeps the lowest
+//     {cost key, lexicographic rank}; O[w], R[w] return the warp's minima
+//     (0xffffffff / kNone: no match of weight w).
+template <bool ML>
+__device__ void small_iteration(const uint32_t *cols, const uint32_t *hcols, const float *llr,
+                                const uint32_t *sw, uint32_t hs, int nwp, int nw, int tam,
+                                const unsigned long long (&wbase)[kMaxW + 1], unsigned wmask,
+                                const unsigned long long *t, unsigned long long &best,
+                                uint32_t (&O)[kMaxW + 1], unsigned long long (&R)[kMaxW + 1]) {
   const int lane = threadIdx.x & 31;
   const int nm = 1 << tam;
   const int per = (nm + 31) >> 5;
   const int g0 = lane * per;
   const int g1 = g0 + per < nm ? g0 + per : nm;
+  best = kNone;
 #pragma unroll
   for (int q = 0; q <= kMaxW; ++q) {
     O[q] = 0xffffffffu;
@@ -304,80 +271,47 @@ __device__ void small_iteration_ml(const uint32_t *cols, const float *llr, const
   }
   if (g0 < g1) {
     unsigned mask = (unsigned)(g0 ^ (g0 >> 1));
-    uint32_t T[NW];
-#pragma unroll
-    for (int i = 0; i < NW; ++i) T[i] = sw[i];
-    for (unsigned mm = mask; mm; mm &= mm - 1u) {
-      uint32_t a[NW];
-      load_words<NW>(cols + (__ffs(mm) - 1) * nwp, a);
-#pragma unroll
-      for (int i = 0; i < NW; ++i) T[i] ^= a[i];
-    }
+    uint32_t h = hs;  // sketch of the syndrome XOR the mask's columns
+    for (unsigned mm = mask; mm; mm &= mm - 1u) h ^= hcols[__ffs(mm) - 1];
     for (int g = g0;;) {
-      uint32_t z = T[0];
-#pragma unroll
-      for (int i = 1; i < NW; ++i) z |= T[i];
-      const int w = __popc(mask);
-      if (z == 0u && ((wmask >> w) & 1u)) {
-        int x[5] = {0, 0, 0, 0, 0};
-        int k = 0, j = 0;
-        float pc = 0.0f;
-        for (unsigned mm = mask; mm; mm &= mm - 1u) {
-          const int bit = __ffs(mm) - 1;
-          pc = __fadd_rn(pc, llr[bit]);
-          if (mm & (mm - 1u)) x[k++] = bit;
-          else j = bit;
-        }
-        const uint32_t o = cost_key(pc);
-        const unsigned long long r = lex_rank(t, tam, w, x, w - 1, j);
-#pragma unroll
-        for (int q = 1; q <= kMaxW; ++q)
-          if (q == w && (o < O[q] || (o == O[q] && r < R[q]))) {
-            O[q] = o;
-            R[q] = r;
+      if (h == 0u) {
+        const int w = __popc(mask);
+        if (((wmask >> w) & 1u) && mask_matches(cols, nwp, nw, sw, mask)) {
+          int x[5] = {0, 0, 0, 0, 0};
+          int k = 0, j = 0;
+          float pc = 0.0f;
+          for (unsigned mm = mask; mm; mm &= mm - 1u) {
+            const int bit = __ffs(mm) - 1;
+            if constexpr (ML) pc = __fadd_rn(pc, llr[bit]);
+            if (mm & (mm - 1u)) x[k++] = bit;
+            else j = bit;
           }
+          const unsigned long long r = lex_rank(t, tam, w, x, w - 1, j);
+          if constexpr (!ML) {
+            const unsigned long long g_idx = wbase[w] + r;
+            if (g_idx < best) best = g_idx;
+          } else {
+            const uint32_t o = cost_key(pc);
+#pragma unroll
+            for (int q = 1; q <= kMaxW; ++q)
+              if (q == w && (o < O[q] || (o == O[q] && r < R[q]))) {
+                O[q] = o;
+                R[q] = r;
+              }
+          }
+        }
       }
       if (++g >= g1) break;
-      const int bit = __ffs(g) - 1;
+      const int bit = __ffs(g) - 1;  // gray(g) ^ gray(g - 1) = 1 << ctz(g)
       mask ^= 1u << bit;
-      uint32_t a[NW];
-      load_words<NW>(cols + bit * nwp, a);
-#pragma unroll
-      for (int i = 0; i < NW; ++i) T[i] ^= a[i];
+      h ^= hcols[bit];
     }
   }
+  if constexpr (!ML) {
+    best = warp_min_u64(best);
+  } else {
 #pragma unroll
-  for (int q = 1; q <= kMaxW; ++q) warp_min_key(O[q], R[q]);
-}
-
-__device__ void small_dispatch_ml(int nw, const uint32_t *cols, const float *llr,
-                                  const uint32_t *sw, int tam, unsigned wmask,
-                                  const unsigned long long *t, uint32_t (&O)[kMaxW + 1],
-                                  unsigned long long (&R)[kMaxW + 1]) {
-  switch (nw) {
-    case 1: small_iteration_ml<1>(cols, llr, sw, tam, wmask, t, O, R); break;
-    case 2: small_iteration_ml<2>(cols, llr, sw, tam, wmask, t, O, R); break;
-    case 3: small_iteration_ml<3>(cols, llr, sw, tam, wmask, t, O, R); break;
-    case 4: small_iteration_ml<4>(cols, llr, sw, tam, wmask, t, O, R); break;
-    case 5: small_iteration_ml<5>(cols, llr, sw, tam, wmask, t, O, R); break;
-    case 6: small_iteration_ml<6>(cols, llr, sw, tam, wmask, t, O, R); break;
-    case 7: small_iteration_ml<7>(cols, llr, sw, tam, wmask, t, O, R); break;
-    default: small_iteration_ml<8>(cols, llr, sw, tam, wmask, t, O, R); break;
-  }
-}
-
-__device__ unsigned long long small_dispatch(int nw, const uint32_t *cols, const uint32_t *sw,
-                                             int tam, const unsigned long long (&wbase)[kMaxW + 1],
-                                             unsigned wmask, const unsigned long long *t) {
-  switch (nw) {
-    case 1: return small_iteration<1>(cols, sw, tam, wbase, wmask, t);
-    case 2: return small_iteration<2>(cols, sw, tam, wbase, wmask, t);
-    case 3: return small_iteration<3>(cols, sw, tam, wbase, wmask, t);
-    case 4: return small_iteration<4>(cols, sw, tam, wbase, wmask, t);
-    case 5: return small_iteration<5>(cols, sw, tam, wbase, wmask, t);
-    case 6: return small_iteration<6>(cols, sw, tam, wbase, wmask, t);
-    case 7: return small_iteration<7>(cols, sw, tam, wbase, wmask, t);
-    default: return small_iteration<8>(cols, sw, tam, wbase, wmask, t);
+    for (int q = 1; q <= kMaxW; ++q) warp_min_key(O[q], R[q]);
   }
 }
 
@@ -389,10 +323,11 @@ __device__ void light_search(const DevBatch &b, const DevCode &cd, Job &J, WarpA
   const int lane = threadIdx.x & 31;
   const bool ml = cd.variant == kMl;
   IterInfo &I = J.it[ii];
-  stage_iteration(cd, A.am[I.src], I.tam, A.pos, A.tmp, A.cols, A.llr);
+  stage_iteration(cd, A.am[I.src], I.tam, A.pos, A.tmp, A.cols, A.hcols, A.llr);
   if (lane == 0) {
     I.pos = A.pos;
     I.cols = A.cols;
+    I.hcols = A.hcols;
     I.llr = A.llr;
     if (ml) {
       float pf = 0.0f;
@@ -404,8 +339,11 @@ __device__ void light_search(const DevBatch &b, const DevCode &cd, Job &J, WarpA
     }
   }
   __syncwarp();
+  const bool small = I.tam <= kSmallTam;
+  uint32_t SO[kMaxW + 1];
+  unsigned long long SR[kMaxW + 1];
   if (!ml) {
-    if (I.tam <= kSmallTam && cd.nw <= 8) {
+    if (small) {
       // weight -> base of the block that searches it first (a later listing of
       // the same weight never matches first)
       unsigned long long wb[kMaxW + 1] = {0, 0, 0, 0, 0, 0, 0};
@@ -416,14 +354,16 @@ __device__ void light_search(const DevBatch &b, const DevCode &cd, Job &J, WarpA
         wb[S.w] = S.base;
         wm |= 1u << S.w;
       }
-      const unsigned long long g = small_dispatch(cd.nw, A.cols, A.sw, I.tam, wb, wm, b.ncr);
+      unsigned long long g;
+      small_iteration<false>(A.cols, A.hcols, A.llr, A.sw, J.hs, cd.nwp, cd.nw, I.tam, wb, wm,
+                             b.ncr, g, SO, SR);
       if (g != kNone) wn = winner_from_index(J, g, cd.variant == kProb);
       return;
     }
     for (int s = I.seg_lo; s < I.seg_hi && !wn.found; ++s) {
       const Seg &S = J.seg[s];
       if (S.dup) continue;
-      SegView sv{A.cols, A.llr, I.tam, S.w, S.K, cd.nwp, cd.nw, S.nprefix, S.base};
+      SegView sv{A.hcols, A.cols, A.llr, J.hs, I.tam, S.w, S.K, cd.nwp, cd.nw, S.nprefix, S.base};
       LaneBest lb;
       lb.reset();
       eval_segment<false>(cd, sv, S, b.ncr, A.sw, lb);
@@ -433,13 +373,13 @@ __device__ void light_search(const DevBatch &b, const DevCode &cd, Job &J, WarpA
     return;
   }
   // upstream search_cpu_ml (grand_decoder.cu:620-656), one weight at a time
-  const bool small = I.tam <= kSmallTam && cd.nw <= 8;
-  uint32_t SO[kMaxW + 1];
-  unsigned long long SR[kMaxW + 1];
   if (small) {
     unsigned wm = 0;
     for (int s = I.seg_lo; s < I.seg_hi; ++s) wm |= 1u << J.seg[s].w;
-    small_dispatch_ml(cd.nw, A.cols, A.llr, A.sw, I.tam, wm, b.ncr, SO, SR);
+    const unsigned long long none[kMaxW + 1] = {0, 0, 0, 0, 0, 0, 0};
+    unsigned long long g;
+    small_iteration<true>(A.cols, A.hcols, A.llr, A.sw, J.hs, cd.nwp, cd.nw, I.tam, none, wm,
+                          b.ncr, g, SO, SR);
   }
   uint32_t bo = 0xffffffffu;
   unsigned long long br = kNone, proc = 0;
@@ -460,7 +400,7 @@ __device__ void light_search(const DevBatch &b, const DevCode &cd, Job &J, WarpA
           r = SR[q];
         }
     } else {
-      SegView sv{A.cols, A.llr, I.tam, S.w, S.K, cd.nwp, cd.nw, S.nprefix, S.base};
+      SegView sv{A.hcols, A.cols, A.llr, J.hs, I.tam, S.w, S.K, cd.nwp, cd.nw, S.nprefix, S.base};
       LaneBest lb;
       lb.reset();
       eval_segment<true>(cd, sv, S, b.ncr, A.sw, lb);
@@ -553,6 +493,12 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
       continue;
     }
 
+    // sketch of the syndrome: XOR of the row hashes of its set rows
+    uint32_t hs = 0u;
+    for (uint32_t word = s_lane; word; word &= word - 1u) hs ^= row_hash(lane * 32 + __ffs(word) - 1);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) hs ^= __shfl_xor_sync(kFull, hs, o);
+
     // ---- flagged-check counts and threshold masks ---------------------------
     const int L = cd.max_soma < kMaxIters ? cd.max_soma : kMaxIters;
     int tam_raw[3] = {0, 0, 0};
@@ -592,6 +538,7 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
       J.original_weight = original_weight;
       J.best = kNone;
       J.tiles_done = 0;
+      J.hs = hs;
       J.t_start = t_start;
       J.t_counts = global_ns();
     }
@@ -637,6 +584,7 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
     for (int ii = heavy_from; ii < J.n_it; ++ii) {
       const unsigned long long tm = (unsigned long long)J.it[ii].tam;
       words += (tm * cd.nwp + 3ull) & ~3ull;              // columns
+      words += (tm + 3ull) & ~3ull;                       // column sketches
       words += ((ml ? 2ull : 1ull) * tm + 3ull) & ~3ull;  // positions (+ sort buffer)
       if (ml) words += (tm + 3ull) & ~3ull;               // LLRs
     }
@@ -668,6 +616,8 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
       const unsigned long long tm = (unsigned long long)I.tam;
       uint32_t *cols = sp;
       sp += (tm * cd.nwp + 3ull) & ~3ull;
+      uint32_t *hcols = sp;
+      sp += (tm + 3ull) & ~3ull;
       int *pos = reinterpret_cast<int *>(sp);
       int *tmp = pos + tm;
       sp += ((ml ? 2ull : 1ull) * tm + 3ull) & ~3ull;
@@ -676,10 +626,11 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
         llr = reinterpret_cast<float *>(sp);
         sp += (tm + 3ull) & ~3ull;
       }
-      stage_iteration(cd, A.am[I.src], I.tam, pos, tmp, cols, llr);
+      stage_iteration(cd, A.am[I.src], I.tam, pos, tmp, cols, hcols, llr);
       if (lane == 0) {
         I.pos = pos;
         I.cols = cols;
+        I.hcols = hcols;
         I.llr = llr;
         if (ml) {
           float pf = 0.0f;
