@@ -337,24 +337,47 @@ __device__ __forceinline__ void eval_run_tile(const SegView &sv, const unsigned 
   const int v = r >= run ? 0 : (int)((run - r) < (unsigned long long)KK ? (run - r) : KK);
 
   const uint32_t hb = sv.hs ^ hc[c];
-  int y[5] = {0, 1, 2, 3, 4};
-  if (v > 0) sub_unrank(t, r, kk, c, y);
-  uint32_t H[KK];  // sketches of s ^ (the lane's prefixes)
-  H[0] = hb;
+  uint32_t H[KK];  // sketches of s ^ (the lane's prefixes); lanes past the run repeat one
+  if (kk == 1) {
+    // weight 3: prefixes {y, c}, y = r, r+1, ...
+    const int y0 = v > 0 ? (int)r : 0;
 #pragma unroll
-  for (int e = 0; e < 5; ++e)
-    if (e < kk) H[0] ^= hc[y[e]];
+    for (int s = 0; s < KK; ++s) H[s] = hb ^ hc[s < v ? y0 + s : y0];
+  } else if (kk == 2) {
+    // weight 4: prefixes {y0, y1, c} in colex order, y0 < y1 < c
+    int y[5] = {0, 1, 2, 3, 4};
+    if (v > 0) sub_unrank(t, r, 2, c, y);
+    int y0 = y[0], y1 = y[1];
+    uint32_t h1 = hb ^ hc[y1];
 #pragma unroll
-  for (int s = 1; s < KK; ++s) {
-    H[s] = H[s - 1];
-    if (s < v) {
-      int old[5];
+    for (int s = 0; s < KK; ++s) {
+      H[s] = h1 ^ hc[y0];
+      if (s + 1 < v) {
+        if (++y0 == y1) {
+          y0 = 0;
+          h1 = hb ^ hc[++y1];
+        }
+      }
+    }
+  } else {
+    int y[5] = {0, 1, 2, 3, 4};
+    if (v > 0) sub_unrank(t, r, kk, c, y);
+    H[0] = hb;
 #pragma unroll
-      for (int e = 0; e < 5; ++e) old[e] = y[e];
-      const int adv = sub_next(y, kk, c);
+    for (int e = 0; e < 5; ++e)
+      if (e < kk) H[0] ^= hc[y[e]];
 #pragma unroll
-      for (int e = 0; e < 5; ++e)
-        if (e < kk && e <= adv && old[e] != y[e]) H[s] ^= hc[old[e]] ^ hc[y[e]];
+    for (int s = 1; s < KK; ++s) {
+      H[s] = H[s - 1];
+      if (s < v) {
+        int old[5];
+#pragma unroll
+        for (int e = 0; e < 5; ++e) old[e] = y[e];
+        const int adv = sub_next(y, kk, c);
+#pragma unroll
+        for (int e = 0; e < 5; ++e)
+          if (e < kk && e <= adv && old[e] != y[e]) H[s] ^= hc[old[e]] ^ hc[y[e]];
+      }
     }
   }
 

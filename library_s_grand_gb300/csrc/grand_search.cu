@@ -117,11 +117,14 @@ __global__ void __launch_bounds__(kSearchThreads, 3) search_kernel(DevBatch b) {
   // spread over every warp.
   const unsigned long long fetch =
       total >= 8ull * kTilesPerFetch * gridDim.x * kSearchWarps ? kTilesPerFetch : 1ull;
+  // the next draw is issued before the current tiles run, so its atomic's
+  // round trip overlaps them
+  unsigned long long draw = 0;
+  if (lane == 0) draw = atomicAdd(&b.counters[1], fetch);
   for (;;) {
-    unsigned long long t0 = 0;
-    if (lane == 0) t0 = atomicAdd(&b.counters[1], fetch);
-    t0 = __shfl_sync(kFull, t0, 0);
+    const unsigned long long t0 = __shfl_sync(kFull, draw, 0);
     if (t0 >= total) break;
+    if (lane == 0) draw = atomicAdd(&b.counters[1], fetch);
     const unsigned long long t1 = (t0 + fetch < total) ? t0 + fetch : total;
     bool skip_known = false, skip = false;
     unsigned long long pending = 0;
@@ -210,22 +213,21 @@ __global__ void __launch_bounds__(kSearchThreads, 3) search_kernel(DevBatch b) {
           if (s_ml) eval_tile<true>(sv, b.ncr, sw, st, lb);
           else eval_tile<false>(sv, b.ncr, sw, st, lb);
         }
+        // a tile without a match (nearly every tile) skips the reductions
         if (!s_ml) {
-          const unsigned long long g = warp_min_u64(lb.g);
-          if (g != kNone) {
+          if (__any_sync(kFull, lb.g != kNone)) {
+            const unsigned long long g = warp_min_u64(lb.g);
             published = true;
             skip_known = false;
             if (lane == 0) atomicMin(&J.best, g);
           }
-        } else {
+        } else if (__any_sync(kFull, lb.o != 0xffffffffu)) {
           uint32_t o = lb.o;
           unsigned long long r = lb.r;
           warp_min_key(o, r);
-          if (o != 0xffffffffu) {
-            published = true;
-            if (lane == 0 && !atomic_min_key(J.mlkey[s_iter][sv.w], o, r))
-              atomicOr(b.status, kStatusCasLimit);
-          }
+          published = true;
+          if (lane == 0 && !atomic_min_key(J.mlkey[s_iter][sv.w], o, r))
+            atomicOr(b.status, kStatusCasLimit);
         }
       }
       // tiles of this fetch done for the current job: posted once per job per fetch

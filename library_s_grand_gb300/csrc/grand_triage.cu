@@ -367,8 +367,8 @@ __device__ void light_search(const DevBatch &b, const DevCode &cd, Job &J, WarpA
       LaneBest lb;
       lb.reset();
       eval_segment<false>(cd, sv, S, b.ncr, A.sw, lb);
-      const unsigned long long g = warp_min_u64(lb.g);
-      if (g != kNone) wn = winner_from_index(J, g, cd.variant == kProb);
+      if (__any_sync(kFull, lb.g != kNone))
+        wn = winner_from_index(J, warp_min_u64(lb.g), cd.variant == kProb);
     }
     return;
   }
