@@ -285,20 +285,34 @@ __device__ __forceinline__ int colex_next(int (&y)[5], int kk, int c) {
   return adv;
 }
 
-// Colex unranking of a kk-subset of [0, c): closed forms for kk <= 2 (weights 3
-// and 4, the common case), the binomial-table search otherwise.
+// Colex unranking of a 2-subset: y1 = largest v with C(v, 2) <= r (from the
+// float square root, then corrected), y0 = the rest.
+__device__ __forceinline__ void unrank2(unsigned long long r, int &y0, int &y1) {
+  int v = (int)((1.0f + sqrtf(1.0f + 8.0f * (float)r)) * 0.5f);
+  if (v < 1) v = 1;
+  while ((unsigned long long)v * (v - 1) / 2 > r) --v;
+  while ((unsigned long long)(v + 1) * v / 2 <= r) ++v;
+  y1 = v;
+  y0 = (int)(r - (unsigned long long)v * (v - 1) / 2);
+}
+
+// Colex unranking of a kk-subset of [0, c): closed forms for kk <= 3 (weights 3
+// to 5, the common case), the binomial-table search otherwise.
 __device__ __forceinline__ void sub_unrank(const unsigned long long *t, unsigned long long r,
                                            int kk, int c, int (&y)[5]) {
   if (kk == 1) {
     y[0] = (int)r;
   } else if (kk == 2) {
-    // largest v with v(v-1)/2 <= r, from the float square root then corrected
-    int v = (int)((1.0f + sqrtf(1.0f + 8.0f * (float)r)) * 0.5f);
-    if (v < 1) v = 1;
-    while ((unsigned long long)v * (v - 1) / 2 > r) --v;
-    while ((unsigned long long)(v + 1) * v / 2 <= r) ++v;
-    y[1] = v;
-    y[0] = (int)(r - (unsigned long long)v * (v - 1) / 2);
+    unrank2(r, y[0], y[1]);
+  } else if (kk == 3) {
+    // largest v with C(v, 3) <= r, from the float cube root, then corrected
+    int v = (int)cbrtf(6.0f * (float)r) + 1;
+    if (v < 2) v = 2;
+    auto c3 = [](int x) { return (unsigned long long)x * (x - 1) * (x - 2) / 6; };
+    while (v > 2 && c3(v) > r) --v;
+    while (c3(v + 1) <= r) ++v;
+    y[2] = v;
+    unrank2(r - c3(v), y[0], y[1]);
   } else {
     colex_unrank(t, r, kk, c - 1, y);
   }
@@ -356,6 +370,27 @@ __device__ __forceinline__ void eval_run_tile(const SegView &sv, const unsigned 
         if (++y0 == y1) {
           y0 = 0;
           h1 = hb ^ hc[++y1];
+        }
+      }
+    }
+  } else if (kk == 3) {
+    // weight 5: prefixes {y0, y1, y2, c} in colex order
+    int y[5] = {0, 1, 2, 3, 4};
+    if (v > 0) sub_unrank(t, r, 3, c, y);
+    int y0 = y[0], y1 = y[1], y2 = y[2];
+    uint32_t h2 = hb ^ hc[y2];
+    uint32_t h1 = h2 ^ hc[y1];
+#pragma unroll
+    for (int s = 0; s < KK; ++s) {
+      H[s] = h1 ^ hc[y0];
+      if (s + 1 < v) {
+        if (++y0 == y1) {
+          y0 = 0;
+          if (++y1 == y2) {
+            y1 = 1;
+            h2 = hb ^ hc[++y2];
+          }
+          h1 = h2 ^ hc[y1];
         }
       }
     }
