@@ -80,6 +80,58 @@ __device__ __forceinline__ void lex_unrank(const unsigned long long *t, unsigned
   }
 }
 
+// Largest i in [lo, hi] with key(i) <= x, for key non-decreasing and
+// key(lo) <= x.  Each step the 32 lanes probe 32 points of the range, so n
+// entries take ceil(log32 n) dependent loads instead of log2 n.
+template <class Key>
+__device__ __forceinline__ int warp_search_le(int lo, int hi, unsigned long long x, Key key) {
+  const int lane = threadIdx.x & 31;
+  while (lo < hi) {
+    const long long span = (long long)hi - lo + 1;
+    const unsigned m = __ballot_sync(kFull, key(lo + (int)((lane * span) >> 5)) <= x);
+    const int l = 31 - __clz(m);  // lane 0 probes lo, so m != 0
+    const int nlo = lo + (int)((l * span) >> 5);
+    hi = (l == 31) ? hi : lo + (int)(((l + 1) * span) >> 5) - 1;
+    lo = nlo;
+  }
+  return lo;
+}
+
+// C(n, k) for k <= 6 by upstream's multiplicative formula (grand_decoder.cu:42-52)
+// with constant divisors: each step r * (n - i + 1) / i is exact and stays below
+// 2^64 for n <= 2048.  No table load, so a chain of them costs no memory latency.
+__device__ __forceinline__ unsigned long long binom(int n, int k) {
+  if (k < 0 || n < k) return 0ull;
+  const unsigned long long m = (unsigned long long)n;
+  unsigned long long r = 1ull;
+  if (k >= 1) r = m;
+  if (k >= 2) r = r * (m - 1ull) / 2ull;
+  if (k >= 3) r = r * (m - 2ull) / 3ull;
+  if (k >= 4) r = r * (m - 3ull) / 4ull;
+  if (k >= 5) r = r * (m - 4ull) / 5ull;
+  if (k >= 6) r = r * (m - 5ull) / 6ull;
+  return r;
+}
+
+// lex_unrank with the whole warp: each element's binomial search probes 32
+// points per step (warp_search_le) and computes the binomials instead of
+// loading them, so a result writer's unranking is a few rounds of ballots with
+// no dependent memory loads.  Every lane gets c.
+__device__ __forceinline__ void lex_unrank_warp(unsigned long long rank, int n, int w,
+                                                int (&c)[kMaxW]) {
+  unsigned long long q = binom(n, w) - 1ull - rank;
+  int hi = n - 1;
+#pragma unroll
+  for (int i = kMaxW; i >= 1; --i) {
+    if (i <= w) {
+      const int v = warp_search_le(i - 1, hi, q, [&](int x) { return binom(x, i); });
+      q -= binom(v, i);
+      c[w - i] = n - 1 - v;
+      hi = v - 1;
+    }
+  }
+}
+
 // Lexicographic rank of prefix x[0..k-1] followed by last index j (k = w - 1).
 __device__ __forceinline__ unsigned long long lex_rank(const unsigned long long *t, int n, int w,
                                                        const int (&x)[5], int k, int j) {
@@ -430,23 +482,21 @@ __device__ __forceinline__ void eval_run_tile(const SegView &sv, const unsigned 
   }
 
   if (v > 0 && acc == 0u) {
-    // A zero sketch among this lane's prefixes: test those candidates word by
-    // word (rare; lanes without valid prefixes only repeat prefix 0's sketch).
-    int yy[5] = {0, 1, 2, 3, 4};
-    sub_unrank(t, r, kk, c, yy);
-    for (int s = 0; s < v; ++s) {
-      if (s > 0) sub_next(yy, kk, c);
-      uint32_t hp = hb;
-      int x[5];
+    // A zero sketch among this lane's prefixes (rare): rescan, and test each
+    // (prefix, j) whose sketch is zero word by word.  Lanes without valid
+    // prefixes only repeat prefix 0's sketch and never get here.
+    for (int j = c + 1; j < tam; ++j) {
+      const uint32_t hj = hc[j];
 #pragma unroll
-      for (int e = 0; e < 5; ++e) {
-        if (e < kk) hp ^= hc[yy[e]];
-        x[e] = (e < kk) ? yy[e] : (e == kk ? c : 0);
-      }
-      for (int j = c + 1; j < tam; ++j) {
-        if ((hp ^ hc[j]) != 0u || !exact_match(sv, sw, x, k, j)) continue;
-        record_match<ML>(sv, t, x, k, j, lb);
-        if constexpr (!ML) break;  // ranks grow with the last index
+      for (int s = 0; s < KK; ++s) {
+        if (s < v && (H[s] ^ hj) == 0u) {
+          int yy[5] = {0, 1, 2, 3, 4};
+          sub_unrank(t, r + (unsigned long long)s, kk, c, yy);
+          int x[5];
+#pragma unroll
+          for (int e = 0; e < 5; ++e) x[e] = (e < kk) ? yy[e] : (e == kk ? c : 0);
+          if (exact_match(sv, sw, x, k, j)) record_match<ML>(sv, t, x, k, j, lb);
+        }
       }
     }
   }

@@ -42,7 +42,7 @@ static __device__ void finish_shot(const DevBatch &b, const DevCode &cd, const J
     const IterInfo &I = J.it[wn.ii];
     w = S.w;
     int c[kMaxW];
-    lex_unrank(b.ncr, wn.rank, I.tam, w, c);
+    lex_unrank_warp(wn.rank, I.tam, w, c);
 #pragma unroll
     for (int i = 0; i < kMaxW; ++i) p[i] = (i < w) ? I.pos[c[i]] : -1;
   } else {
@@ -69,17 +69,36 @@ static __device__ void finish_shot(const DevBatch &b, const DevCode &cd, const J
     // (grand_decoder.cu:456-474).  In reduced row echelon form the vector's own
     // bits at pivot columns decide alone which rows upstream adds, so the test
     // is delta == XOR of the rows pivoted on delta's set bits.
+    // Each lane looks up the pivot row of one set bit of a delta word, then the
+    // warp XORs those rows four at a time (their loads issued together).
     uint32_t acc[4] = {0u, 0u, 0u, 0u};  // words lane, lane+32, lane+64, lane+96
     for (int q = 0; q < cd.mw; ++q) {
-      uint32_t word = delta[q];
-      while (word) {
-        const int c = q * 32 + __ffs(word) - 1;
-        word &= word - 1u;
-        const int r = __ldg(cd.pivrow + c);
-        if (r < 0) continue;
+      const uint32_t word = delta[q];
+      if (word == 0u) continue;
+      const int r = ((word >> lane) & 1u) ? __ldg(cd.pivrow + q * 32 + lane) : -1;
+      unsigned m = __ballot_sync(kFull, r >= 0);
+      while (m) {
+        int rb[4];
 #pragma unroll
-        for (int k = 0; k < 4; ++k)
-          if (lane + 32 * k < cd.mw) acc[k] ^= __ldg(cd.rref + (size_t)r * cd.mw + lane + 32 * k);
+        for (int u = 0; u < 4; ++u) {
+          rb[u] = -1;
+          if (m) {
+            rb[u] = __shfl_sync(kFull, r, __ffs(m) - 1);
+            m &= m - 1u;
+          }
+        }
+        uint32_t v[4][4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+          for (int k = 0; k < 4; ++k)
+            v[u][k] = (rb[u] >= 0 && lane + 32 * k < cd.mw)
+                          ? __ldg(cd.rref + (size_t)rb[u] * cd.mw + lane + 32 * k)
+                          : 0u;
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+          for (int k = 0; k < 4; ++k) acc[k] ^= v[u][k];
       }
     }
     bool ok = true;

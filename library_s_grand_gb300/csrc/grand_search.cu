@@ -16,23 +16,6 @@ namespace grand {
 // ---------------------------------------------------------------------------
 // Kernel 2: persistent work-stealing search over the Jobs' tiles.
 // ---------------------------------------------------------------------------
-// Largest i in [lo, hi] with key(i) <= x, for key non-decreasing and
-// key(lo) <= x.  Each step the 32 lanes probe 32 points of the range, so n
-// entries take ceil(log32 n) dependent loads instead of log2 n.
-template <class Key>
-__device__ __forceinline__ int warp_search_le(int lo, int hi, unsigned long long x, Key key) {
-  const int lane = threadIdx.x & 31;
-  while (lo < hi) {
-    const long long span = (long long)hi - lo + 1;
-    const unsigned m = __ballot_sync(kFull, key(lo + (int)((lane * span) >> 5)) <= x);
-    const int l = 31 - __clz(m);  // lane 0 probes lo, so m != 0
-    const int nlo = lo + (int)((l * span) >> 5);
-    hi = (l == 31) ? hi : lo + (int)(((l + 1) * span) >> 5) - 1;
-    lo = nlo;
-  }
-  return lo;
-}
-
 __device__ bool tile_skip(const Job &J, const Seg &S, const IterInfo &I, bool ml) {
   if (!ml) {
     const unsigned long long best = *reinterpret_cast<const volatile unsigned long long *>(&J.best);
