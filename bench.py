@@ -354,7 +354,7 @@ STRESS_SHOTS = 192
 SKETCH_OPS_PER_CANDIDATE = 1.5
 # DRAM bytes (read + write) of one search_kernel launch on the stress input, from an ncu
 # --set full capture of `bench.py --case stress` (48 shots), scaled to 192 shots.
-STRESS_TRAFFIC_PER_SHOT = (1.164288e6 + 133.888e3) / 48
+STRESS_TRAFFIC_PER_SHOT = (1.019136e6 + 47.36e3) / 48
 
 
 def stress_case(torch, lib, dev, n=STRESS_SHOTS):

@@ -38,6 +38,22 @@ __device__ __forceinline__ unsigned long long ncr(const unsigned long long *t, i
   return __ldg(t + n * (kMaxW + 1) + k);
 }
 
+// C(n, k) for k <= 6 by upstream's multiplicative formula (grand_decoder.cu:42-52)
+// with constant divisors: each step r * (n - i + 1) / i is exact and stays below
+// 2^64 for n <= 2048.  No table load, so a chain of them costs no memory latency.
+__device__ __forceinline__ unsigned long long binom(int n, int k) {
+  if (k < 0 || n < k) return 0ull;
+  const unsigned long long m = (unsigned long long)n;
+  unsigned long long r = 1ull;
+  if (k >= 1) r = m;
+  if (k >= 2) r = r * (m - 1ull) / 2ull;
+  if (k >= 3) r = r * (m - 2ull) / 3ull;
+  if (k >= 4) r = r * (m - 3ull) / 4ull;
+  if (k >= 5) r = r * (m - 4ull) / 5ull;
+  if (k >= 6) r = r * (m - 5ull) / 6ull;
+  return r;
+}
+
 // Largest v in [lo, hi] with C(v, k) <= q (C(v, k) is non-decreasing in v there).
 __device__ __forceinline__ int ncr_floor(const unsigned long long *t, unsigned long long q, int k,
                                          int lo, int hi) {
@@ -95,22 +111,6 @@ __device__ __forceinline__ int warp_search_le(int lo, int hi, unsigned long long
     lo = nlo;
   }
   return lo;
-}
-
-// C(n, k) for k <= 6 by upstream's multiplicative formula (grand_decoder.cu:42-52)
-// with constant divisors: each step r * (n - i + 1) / i is exact and stays below
-// 2^64 for n <= 2048.  No table load, so a chain of them costs no memory latency.
-__device__ __forceinline__ unsigned long long binom(int n, int k) {
-  if (k < 0 || n < k) return 0ull;
-  const unsigned long long m = (unsigned long long)n;
-  unsigned long long r = 1ull;
-  if (k >= 1) r = m;
-  if (k >= 2) r = r * (m - 1ull) / 2ull;
-  if (k >= 3) r = r * (m - 2ull) / 3ull;
-  if (k >= 4) r = r * (m - 3ull) / 4ull;
-  if (k >= 5) r = r * (m - 4ull) / 5ull;
-  if (k >= 6) r = r * (m - 5ull) / 6ull;
-  return r;
 }
 
 // lex_unrank with the whole warp: each element's binomial search probes 32
@@ -239,7 +239,8 @@ __device__ __forceinline__ void eval_tile(const SegView &sv, const unsigned long
   uint32_t h = sv.hs;
   int clast = -1;
   if (valid && k > 0) {
-    colex_unrank(t, q, k, tam - 2, x);
+    if (k == 1) x[0] = (int)q;  // a 1-subset's colex rank is its element
+    else colex_unrank(t, q, k, tam - 2, x);
 #pragma unroll
     for (int i = 0; i < 5; ++i)
       if (i < k) {
@@ -505,7 +506,7 @@ __device__ __forceinline__ void eval_run_tile(const SegView &sv, const unsigned 
 // Number of run tiles of run c for weight w (KK prefixes per lane).
 __device__ __forceinline__ unsigned long long run_tiles(const unsigned long long *t, int c, int w,
                                                         int KK) {
-  const unsigned long long n = ncr(t, c, w - 2);
+  const unsigned long long n = binom(c, w - 2);
   const unsigned long long per = 32ull * (unsigned long long)KK;
   return (n + per - 1ull) / per;
 }
