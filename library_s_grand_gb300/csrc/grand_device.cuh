@@ -126,7 +126,9 @@ __device__ __forceinline__ void lex_unrank_warp(unsigned long long rank, int n, 
     if (i <= w) {
       const int v = warp_search_le(i - 1, hi, q, [&](int x) { return binom(x, i); });
       q -= binom(v, i);
-      c[w - i] = n - 1 - v;
+#pragma unroll
+      for (int e = 0; e < kMaxW; ++e)  // c[w - i], with constant indices
+        if (e == w - i) c[e] = n - 1 - v;
       hi = v - 1;
     }
   }

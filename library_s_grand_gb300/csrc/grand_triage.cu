@@ -40,12 +40,12 @@ struct PlanState {
   unsigned long long gbase;
 };
 
-__device__ int plan_next(const DevCode &cd, const unsigned long long *t, const int (&tam_raw)[3],
-                         int L, int tile_k, Job &J, PlanState &P) {
+__device__ int plan_next(const DevCode &cd, int tam0, int tam1, int tam2, int L, int tile_k, Job &J,
+                         PlanState &P) {
   while (P.i < L) {
     const int i = P.i++;
     P.passes = i + 1;
-    int tam = tam_raw[i];
+    int tam = i == 0 ? tam0 : (i == 1 ? tam1 : tam2);
     if (cd.family == kDem) {  // grand_decoder.cu:1550-1554
       if (tam > cd.cap) tam = P.tam_old;
       else P.tam_old = tam;
@@ -68,7 +68,26 @@ __device__ int plan_next(const DevCode &cd, const unsigned long long *t, const i
     I.base = P.gbase;
     I.phase_end[0] = I.phase_end[1] = I.phase_end[2] = 0;
     unsigned long long tot = 0;
-    int wl[kMaxSegsPerIter], ph[kMaxSegsPerIter], nwl = 0;
+    unsigned seen = 0;
+    // one weight block of weight w in phase position k, appended in search order
+    auto emit = [&](int w, int k) {
+      Seg &S = J.seg[J.nseg++];
+      S.iter = J.n_it;
+      S.w = w;
+      S.phase = k;
+      S.dup = (seen >> w) & 1u;
+      seen |= 1u << w;
+      S.count = binom(tam, w);
+      S.base = P.gbase + tot;
+      S.nprefix = binom(tam - 1, w - 1);
+      S.runs = w >= 3 ? 1 : 0;
+      S.cum = nullptr;
+      S.K = S.runs ? kRunKK : tile_k;
+      // run-tile counts are built by the warp when a Job is published
+      S.ntiles = S.runs ? 0ull : (S.nprefix + 32ull * S.K - 1) / (32ull * S.K);
+      tot += S.count;
+      if (cd.variant == kProb) I.phase_end[k] = tot;
+    };
     if (cd.variant == kProb) {
       int mi = cd.n_masks - 1;  // grand_decoder.cu:754-762
       for (int q = 0; q < cd.n_masks; ++q)
@@ -76,33 +95,14 @@ __device__ int plan_next(const DevCode &cd, const unsigned long long *t, const i
       for (int k = 0; k < cd.num_phases; ++k) {  // grand_decoder.cu:764-786
         const int pid = cd.mask_order[mi][k];
         if (pid == 0) {
-          for (int w = 1; w <= 5 && w <= tam && w <= kMaxW; ++w) { wl[nwl] = w; ph[nwl++] = k; }
+          for (int w = 1; w <= 5 && w <= tam && w <= kMaxW; ++w) emit(w, k);
         } else if (pid == 1) {
-          if (6 <= tam && 6 <= kMaxW) { wl[nwl] = 6; ph[nwl++] = k; }
+          if (6 <= tam && 6 <= kMaxW) emit(6, k);
         }
       }
     } else {
       const int wmax = cd.Wc < tam ? cd.Wc : tam;
-      for (int w = 1; w <= wmax; ++w) { wl[nwl] = w; ph[nwl++] = 0; }
-    }
-    unsigned seen = 0;
-    for (int q = 0; q < nwl; ++q) {
-      Seg &S = J.seg[J.nseg++];
-      S.iter = J.n_it;
-      S.w = wl[q];
-      S.phase = ph[q];
-      S.dup = (seen >> S.w) & 1u;
-      seen |= 1u << S.w;
-      S.count = ncr(t, tam, S.w);
-      S.base = P.gbase + tot;
-      S.nprefix = ncr(t, tam - 1, S.w - 1);
-      S.runs = S.w >= 3 ? 1 : 0;
-      S.cum = nullptr;
-      S.K = S.runs ? kRunKK : tile_k;
-      // run-tile counts are built by the warp when a Job is published
-      S.ntiles = S.runs ? 0ull : (S.nprefix + 32ull * S.K - 1) / (32ull * S.K);
-      tot += S.count;
-      if (cd.variant == kProb) I.phase_end[S.phase] = tot;
+      for (int w = 1; w <= wmax; ++w) emit(w, 0);
     }
     if (cd.variant == kProb)  // phases without weights keep the running total
       for (int k = 1; k < 3; ++k)
@@ -278,17 +278,29 @@ __device__ void small_iteration(const uint32_t *cols, const uint32_t *hcols, con
         const int w = __popc(mask);
         if (((wmask >> w) & 1u) && mask_matches(cols, nwp, nw, sw, mask)) {
           int x[5] = {0, 0, 0, 0, 0};
-          int k = 0, j = 0;
+          int j = 0;
           float pc = 0.0f;
-          for (unsigned mm = mask; mm; mm &= mm - 1u) {
-            const int bit = __ffs(mm) - 1;
-            if constexpr (ML) pc = __fadd_rn(pc, llr[bit]);
-            if (mm & (mm - 1u)) x[k++] = bit;
-            else j = bit;
+          unsigned mm = mask;
+#pragma unroll
+          for (int e = 0; e < 6; ++e) {  // set bits in ascending order; the last is j
+            if (mm) {
+              const int bit = __ffs(mm) - 1;
+              mm &= mm - 1u;
+              if constexpr (ML) pc = __fadd_rn(pc, llr[bit]);
+              if (mm) {
+                if (e < 5) x[e < 5 ? e : 4] = bit;
+              } else {
+                j = bit;
+              }
+            }
           }
           const unsigned long long r = lex_rank(t, tam, w, x, w - 1, j);
           if constexpr (!ML) {
-            const unsigned long long g_idx = wbase[w] + r;
+            unsigned long long wbw = 0;
+#pragma unroll
+            for (int q = 1; q <= kMaxW; ++q)
+              if (q == w) wbw = wbase[q];
+            const unsigned long long g_idx = wbw + r;
             if (g_idx < best) best = g_idx;
           } else {
             const uint32_t o = cost_key(pc);
@@ -351,7 +363,9 @@ __device__ void light_search(const DevBatch &b, const DevCode &cd, Job &J, WarpA
       for (int s = I.seg_lo; s < I.seg_hi; ++s) {
         const Seg &S = J.seg[s];
         if (S.dup) continue;
-        wb[S.w] = S.base;
+#pragma unroll
+        for (int q = 1; q <= kMaxW; ++q)  // constant indices keep wb in registers
+          if (q == S.w) wb[q] = S.base;
         wm |= 1u << S.w;
       }
       unsigned long long g;
@@ -555,7 +569,7 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
     int heavy_from = -1;
     for (;;) {
       int more = 0;
-      if (lane == 0) more = plan_next(cd, b.ncr, tam_raw, L, b.tile_k, J, P);
+      if (lane == 0) more = plan_next(cd, tam_raw[0], tam_raw[1], tam_raw[2], L, b.tile_k, J, P);
       more = __shfl_sync(kFull, more, 0);
       __syncwarp();
       if (!more) break;
@@ -564,7 +578,7 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
       if (I.total > budget || I.tam > kLightTam || I.tam * cd.nwp > kLightWords) {
         heavy_from = ii;
         if (lane == 0)
-          while (plan_next(cd, b.ncr, tam_raw, L, b.tile_k, J, P)) {
+          while (plan_next(cd, tam_raw[0], tam_raw[1], tam_raw[2], L, b.tile_k, J, P)) {
           }
         __syncwarp();
         break;
