@@ -281,10 +281,15 @@ def run_ours(args):
         total_ms = float(t.item())
     value = world * SHOTS * args.steps / (total_ms * 1e-3)
 
-    # kernel split (non-graph launch with events)
-    eng.decode_device(SHOTS, d_rec.data_ptr(), d_res.data_ptr(), sp, use_graph=False)
-    eng.sync_status(sp)
-    tri_ms, sea_ms = eng.kernel_times(sp)
+    # kernel split (non-graph launches with events; median of 5)
+    split = []
+    for _ in range(5):
+        flush.fill_(7)
+        eng.decode_device(SHOTS, d_rec.data_ptr(), d_res.data_ptr(), sp, use_graph=False)
+        eng.sync_status(sp)
+        split.append(eng.kernel_times(sp))
+    tri_ms, sea_ms = (float(np.median([x[i] for x in split])) for i in range(2))
+    hbm = hbm_streaming(code, tri_ms)
 
     out = None
     if rank == 0:
@@ -340,7 +345,7 @@ def run_ours(args):
             "plain_what": "one call per shot: H2D record, triage+search launches, sync, D2H",
             "persistent_vs_plain": value / world / (n_plain / plain_s),
             "kernel_ms": {"triage": tri_ms, "search": sea_ms},
-            "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
+            "e2e": e2e, "roofline": roof, "hbm_streaming": hbm, "cpu_baseline": cpu, "clocks": clk,
             "gpu_launches": 2 * args.steps,
         }
         out.update(extra)
@@ -348,6 +353,34 @@ def run_ours(args):
         dist.barrier()
         dist.destroy_process_group()
     return out
+
+
+# DRAM bytes (read + write) of one triage_kernel launch on the headline batch, from an ncu
+# --set full capture of `bench.py --case headline`.
+TRIAGE_TRAFFIC = 9.591552e6 + 26.368e3
+
+
+def hbm_peak():
+    """Measured copy bandwidth of the GB300s (MEASURED_PEAKS.json), else the fallback."""
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")
+    try:
+        with open(path, encoding="utf-8") as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, ValueError, KeyError):
+        return 6800.0, "fallback"
+
+
+def hbm_streaming(code, tri_ms):
+    """Record streaming of the triage kernel on the headline batch: int32 error records in
+    (4m bytes per shot) and 72-byte results out, per launch, over the kernel's event time."""
+    peak, src = hbm_peak()
+    per_shot = 4 * code.m + 72
+    gbs = SHOTS * per_shot / (tri_ms * 1e-3) / 1e9
+    return {"kernel": "triage_kernel", "achieved": gbs, "peak": peak, "unit": "GB/s",
+            "frac": gbs / peak, "peak_source": src + " copy bandwidth (MEASURED_PEAKS.json)",
+            "algorithmic_bytes_per_launch": SHOTS * per_shot, "traffic": TRIAGE_TRAFFIC,
+            "traffic_unit": "bytes per launch (ncu)", "triage_ms": tri_ms,
+            "what": "bytes per launch: int32 error records (4m per shot) + 72-byte results"}
 
 
 STRESS_SHOTS = 192

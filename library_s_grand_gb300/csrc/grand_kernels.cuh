@@ -30,6 +30,7 @@ struct Winner {
   unsigned long long rank;  // lexicographic rank inside the weight block
   unsigned long long count; // candidates the winning iteration reports
   float cost;
+  unsigned mask;            // the winner's active positions as a bit mask (0: from rank)
 };
 
 static __device__ void finish_shot(const DevBatch &b, const DevCode &cd, const Job &J, int shot,
@@ -42,7 +43,16 @@ static __device__ void finish_shot(const DevBatch &b, const DevCode &cd, const J
     const IterInfo &I = J.it[wn.ii];
     w = S.w;
     int c[kMaxW];
-    lex_unrank_warp(wn.rank, I.tam, w, c);
+    if (wn.mask) {  // the small-set path hands over the positions themselves
+      unsigned mm = wn.mask;
+#pragma unroll
+      for (int i = 0; i < kMaxW; ++i) {
+        c[i] = mm ? __ffs(mm) - 1 : 0;
+        mm &= mm - 1u;
+      }
+    } else {
+      lex_unrank_warp(wn.rank, I.tam, w, c);
+    }
 #pragma unroll
     for (int i = 0; i < kMaxW; ++i) p[i] = (i < w) ? I.pos[c[i]] : -1;
   } else {
@@ -65,6 +75,10 @@ static __device__ void finish_shot(const DevBatch &b, const DevCode &cd, const J
     }
     is_equal = __all_sync(kFull, eq) ? 1 : 0;
     __syncwarp();
+  }
+  if (is_equal) {
+    degenerate = 1;  // delta = 0 lies in every row space
+  } else if (wn.found && cd.family == kCss && cd.input_kind == kInErrors) {
     // degenerate: (e ^ e_est) in the row space of the other matrix
     // (grand_decoder.cu:456-474).  In reduced row echelon form the vector's own
     // bits at pivot columns decide alone which rows upstream adds, so the test
@@ -135,36 +149,44 @@ static __device__ void finish_shot(const DevBatch &b, const DevCode &cd, const J
     }
   }
 
+  // The 72-byte result, written by lanes 0..17 as one coalesced store of 32-bit
+  // words (every lane holds the same fields; lane l stores word l).
+  int h = -2;
+  unsigned long long tested = 0;
+  const int last = wn.found ? wn.ii : J.n_it - 1;
+  for (int k = 0; k <= last; ++k) {
+    h = (J.it[k].branch == kBranchGpu) ? (h == -1 ? 1 : 0) : -1;
+    if (k < last || !wn.found) tested += J.it[k].total;
+  }
+  if (wn.found) tested += wn.count;
+  // Per-shot times from the global timer: the flagged-check count step, the
+  // search from its end to this result (light search, plus queueing and the
+  // search kernel for a published Job), and, when found, the whole shot.
+  // Records move in one batch (or are read in place), so no copy time is
+  // attributed to a shot.  Lanes 10..17 each convert the double they store.
+  const unsigned long long now = __shfl_sync(kFull, global_ns(), 0);
+  const unsigned long long dt = lane < 12   ? J.t_counts - J.t_start
+                                : lane < 14 ? now - J.t_counts
+                                : lane < 16 ? 0ull
+                                            : (wn.found ? now - J.t_start : 0ull);
+  const unsigned long long dbits = (unsigned long long)__double_as_longlong(1e-6 * (double)dt);
+  uint32_t v = 0;
+  switch (lane) {
+    case 0: v = (uint32_t)wn.found; break;
+    case 1: v = (uint32_t)w; break;
+    case 2: v = (uint32_t)J.original_weight; break;
+    case 3: v = (uint32_t)degenerate; break;
+    case 4: v = (uint32_t)is_equal; break;
+    case 5: v = (uint32_t)(wn.found ? J.it[wn.ii].tam : J.final_tam); break;
+    case 6: v = (uint32_t)tested; break;
+    case 7: v = (uint32_t)(tested >> 32); break;
+    case 8: v = (uint32_t)h; break;
+    case 9: v = (uint32_t)(wn.found ? J.it[wn.ii].it : J.final_iteration); break;
+    default: v = (lane & 1) ? (uint32_t)(dbits >> 32) : (uint32_t)dbits; break;
+  }
+  static_assert(sizeof(GrandDecoderResult) == 72, "result layout");
+  if (lane < 18) reinterpret_cast<uint32_t *>(b.results + shot)[lane] = v;
   if (lane == 0) {
-    int h = -2;
-    unsigned long long tested = 0;
-    const int last = wn.found ? wn.ii : J.n_it - 1;
-    for (int k = 0; k <= last; ++k) {
-      h = (J.it[k].branch == kBranchGpu) ? (h == -1 ? 1 : 0) : -1;
-      if (k < last || !wn.found) tested += J.it[k].total;
-    }
-    if (wn.found) tested += wn.count;
-    GrandDecoderResult r;
-    r.found = wn.found;
-    r.found_weight = w;
-    r.original_weight = J.original_weight;
-    r.degenerate = degenerate;
-    r.is_equal = is_equal;
-    r.tam = wn.found ? J.it[wn.ii].tam : J.final_tam;
-    r.total_tested_combinations = tested;
-    r.hibrido = h;
-    r.iteration = wn.found ? J.it[wn.ii].it : J.final_iteration;
-    // Per-shot times from the global timer: the flagged-check count step, the
-    // search from its end to this result (light search, plus queueing and the
-    // search kernel for a published Job), and, when found, the whole shot.
-    // Records move in one batch (or are read in place), so no copy time is
-    // attributed to a shot.
-    const unsigned long long now = global_ns();
-    r.time_sum_ms = 1e-6 * (double)(J.t_counts - J.t_start);
-    r.total_time_search_ms = 1e-6 * (double)(now - J.t_counts);
-    r.transfer_time_ms = 0.0;
-    r.total_to_find_ms = wn.found ? 1e-6 * (double)(now - J.t_start) : 0.0;
-    b.results[shot] = r;
     if (b.ml_cost) b.ml_cost[shot] = wn.found ? wn.cost : 0.0f;
     if (J.failed) atomicOr(b.status, kStatusTamLimit);
   }
@@ -177,6 +199,7 @@ static __device__ Winner winner_from_index(const Job &J, unsigned long long g, b
   wn.ii = wn.seg = 0;
   wn.rank = wn.count = 0;
   wn.cost = 0.0f;
+  wn.mask = 0u;
   if (g == kNone) return wn;
   for (int ii = 0; ii < J.n_it; ++ii) {
     const IterInfo &I = J.it[ii];

@@ -39,6 +39,7 @@ __device__ Winner winner_ml(const Job &J) {
   wn.ii = wn.seg = 0;
   wn.rank = wn.count = 0;
   wn.cost = 0.0f;
+  wn.mask = 0u;
   for (int ii = J.it_lo; ii < J.n_it; ++ii) {
     const IterInfo &I = J.it[ii];
     uint32_t bo = 0xffffffffu;

@@ -257,13 +257,15 @@ __device__ void small_iteration(const uint32_t *cols, const uint32_t *hcols, con
                                 const uint32_t *sw, uint32_t hs, int nwp, int nw, int tam,
                                 const unsigned long long (&wbase)[kMaxW + 1], unsigned wmask,
                                 const unsigned long long *t, unsigned long long &best,
-                                uint32_t (&O)[kMaxW + 1], unsigned long long (&R)[kMaxW + 1]) {
+                                unsigned &bmask, uint32_t (&O)[kMaxW + 1],
+                                unsigned long long (&R)[kMaxW + 1]) {
   const int lane = threadIdx.x & 31;
   const int nm = 1 << tam;
   const int per = (nm + 31) >> 5;
   const int g0 = lane * per;
   const int g1 = g0 + per < nm ? g0 + per : nm;
   best = kNone;
+  unsigned lmask = 0u;
 #pragma unroll
   for (int q = 0; q <= kMaxW; ++q) {
     O[q] = 0xffffffffu;
@@ -301,7 +303,10 @@ __device__ void small_iteration(const uint32_t *cols, const uint32_t *hcols, con
             for (int q = 1; q <= kMaxW; ++q)
               if (q == w) wbw = wbase[q];
             const unsigned long long g_idx = wbw + r;
-            if (g_idx < best) best = g_idx;
+            if (g_idx < best) {
+              best = g_idx;
+              lmask = mask;
+            }
           } else {
             const uint32_t o = cost_key(pc);
 #pragma unroll
@@ -320,7 +325,13 @@ __device__ void small_iteration(const uint32_t *cols, const uint32_t *hcols, con
     }
   }
   if constexpr (!ML) {
+    // the lane holding the lowest index hands its mask over (each mask is
+    // visited by exactly one lane, so the index identifies one lane)
+    const unsigned long long lbest = best;
     best = warp_min_u64(best);
+    const unsigned who = __ballot_sync(kFull, best != kNone && lbest == best);
+    bmask = __shfl_sync(kFull, lmask, who ? __ffs(who) - 1 : 0);
+    if (!who) bmask = 0u;
   } else {
 #pragma unroll
     for (int q = 1; q <= kMaxW; ++q) warp_min_key(O[q], R[q]);
@@ -369,9 +380,13 @@ __device__ void light_search(const DevBatch &b, const DevCode &cd, Job &J, WarpA
         wm |= 1u << S.w;
       }
       unsigned long long g;
+      unsigned gm;
       small_iteration<false>(A.cols, A.hcols, A.llr, A.sw, J.hs, cd.nwp, cd.nw, I.tam, wb, wm,
-                             b.ncr, g, SO, SR);
-      if (g != kNone) wn = winner_from_index(J, g, cd.variant == kProb);
+                             b.ncr, g, gm, SO, SR);
+      if (g != kNone) {
+        wn = winner_from_index(J, g, cd.variant == kProb);
+        wn.mask = gm;
+      }
       return;
     }
     for (int s = I.seg_lo; s < I.seg_hi && !wn.found; ++s) {
@@ -392,8 +407,9 @@ __device__ void light_search(const DevBatch &b, const DevCode &cd, Job &J, WarpA
     for (int s = I.seg_lo; s < I.seg_hi; ++s) wm |= 1u << J.seg[s].w;
     const unsigned long long none[kMaxW + 1] = {0, 0, 0, 0, 0, 0, 0};
     unsigned long long g;
+    unsigned gm;
     small_iteration<true>(A.cols, A.hcols, A.llr, A.sw, J.hs, cd.nwp, cd.nw, I.tam, none, wm,
-                          b.ncr, g, SO, SR);
+                          b.ncr, g, gm, SO, SR);
   }
   uint32_t bo = 0xffffffffu;
   unsigned long long br = kNone, proc = 0;
@@ -566,6 +582,7 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
     wn.ii = wn.seg = 0;
     wn.rank = wn.count = 0;
     wn.cost = 0.0f;
+    wn.mask = 0u;
     int heavy_from = -1;
     for (;;) {
       int more = 0;
