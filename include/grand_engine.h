@@ -90,6 +90,14 @@ int grand_engine_set_tuning(GrandEngine *engine, int light_log2, int tile_k,
 int grand_engine_kernel_times(GrandEngine *engine, void *stream, float *triage_ms,
                               float *search_ms);
 
+/* Times of the last host-buffer decode (grand_engine_decode / _decode_plain):
+ * copies in, the triage kernel(s), the search kernel(s) and copies out, from
+ * CUDA events on the call's stream.  With zero-copy (records read and results
+ * written in place over NVLink-C2C) the copy times are ~0 and the kernels'
+ * times include reading host memory.  Any pointer may be NULL. */
+int grand_engine_batch_times(GrandEngine *engine, float *h2d_ms, float *triage_ms,
+                             float *search_ms, float *d2h_ms);
+
 /* Diagnostic: sustained 32-bit logic-op (lop3) issue rate of the current device
  * in ops/s, the ceiling of the search kernel's integer roofline; < 0 on error. */
 double grand_measure_int_peak(void);

@@ -194,6 +194,10 @@ int grand_engine_decode(GrandEngine *e, int num_shots, const int *shot_code, con
   if (out && out->ml_cost) req.h_cost = out->ml_cost;
   BatchTiming t;
   int rc = run_batch(e->ctx, ws, req, &t, &e->tn);
+  {
+    std::lock_guard<std::mutex> lk(e->mu);
+    e->last = t;
+  }
   e->ctx->release(ws);
   return rc;
 }
@@ -304,6 +308,17 @@ int grand_engine_sync_status(GrandEngine *e, void *stream) {
     return GRAND_ERR_LIMIT;
   }
   if (st & kStatusCasLimit) return GRAND_ERR_CUDA;
+  return 0;
+}
+
+int grand_engine_batch_times(GrandEngine *e, float *h2d_ms, float *triage_ms, float *search_ms,
+                             float *d2h_ms) {
+  if (!e) return GRAND_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(e->mu);
+  if (h2d_ms) *h2d_ms = e->last.h2d_ms;
+  if (triage_ms) *triage_ms = e->last.triage_ms;
+  if (search_ms) *search_ms = e->last.search_ms;
+  if (d2h_ms) *d2h_ms = e->last.d2h_ms;
   return 0;
 }
 

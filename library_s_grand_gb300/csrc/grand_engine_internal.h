@@ -53,6 +53,7 @@ struct GrandEngine {
   grand::Tuning tn;
   std::map<const void *, grand::EngineSlot *> slots;  // per stream
   std::map<grand::GraphKey, cudaGraphExec_t> graphs;
+  grand::BatchTiming last{};  // times of the last host-buffer decode
   ~GrandEngine() {
     for (auto &g : graphs) cudaGraphExecDestroy(g.second);
     for (auto &s : slots) delete s.second;

@@ -30,6 +30,7 @@ _SIGS = {
     "grand_engine_set_tuning": ([VP, ctypes.c_int, ctypes.c_int, ctypes.c_int], ctypes.c_int),
     "grand_engine_kernel_times": ([VP, VP, ctypes.POINTER(ctypes.c_float),
                                    ctypes.POINTER(ctypes.c_float)], ctypes.c_int),
+    "grand_engine_batch_times": ([VP] + [ctypes.POINTER(ctypes.c_float)] * 4, ctypes.c_int),
     "grand_measure_int_peak": ([], ctypes.c_double),
     "grand_device_info": ([ctypes.c_char_p, ctypes.c_int], ctypes.c_int),
 }
@@ -143,6 +144,12 @@ class Engine:
         a, b = ctypes.c_float(), ctypes.c_float()
         rc = self.lib.grand_engine_kernel_times(self.h, stream or None, ctypes.byref(a), ctypes.byref(b))
         return (a.value, b.value) if rc == 0 else (None, None)
+
+    def batch_times(self):
+        """(h2d, triage, search, d2h) ms of the last host-buffer decode."""
+        v = [ctypes.c_float() for _ in range(4)]
+        rc = self.lib.grand_engine_batch_times(self.h, *[ctypes.byref(x) for x in v])
+        return tuple(x.value for x in v) if rc == 0 else None
 
     def int_peak(self):
         return self.lib.grand_measure_int_peak()
