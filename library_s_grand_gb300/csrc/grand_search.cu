@@ -96,11 +96,13 @@ __global__ void __launch_bounds__(kSearchThreads, 3) search_kernel(DevBatch b) {
   int s_runs = 0, s_iter = 0, s_ml = 0, s_prob = 0;
   const unsigned long long *s_cum = nullptr;
 
-  // Tiles are drawn kTilesPerFetch at a time when there are many per warp, one
-  // at a time when there are few, so that a handful of expensive Jobs still
-  // spread over every warp.
-  const unsigned long long fetch =
-      total >= 8ull * kTilesPerFetch * gridDim.x * kSearchWarps ? kTilesPerFetch : 1ull;
+  // Tiles are drawn several at a time when there are many per warp (the
+  // lookups and the Job's tile count are then paid once per draw), one at a
+  // time when there are few, so that a handful of expensive Jobs still spread
+  // over every warp: the largest power of two up to kTilesPerFetch that leaves
+  // each warp at least 8 draws.
+  unsigned long long fetch = kTilesPerFetch;
+  while (fetch > 1ull && total < 8ull * fetch * gridDim.x * kSearchWarps) fetch >>= 1;
   // the next draw is issued before the current tiles run, so its atomic's
   // round trip overlaps them
   unsigned long long draw = 0;
