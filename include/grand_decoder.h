@@ -175,6 +175,32 @@ int grand_decode_cc_noalloc(const int *d_H, int n, int m, const int *d_syndromes
                             void *stream);
 
 /* Library version string and last error message of the calling thread. */
+/* ---------------------------------------------------------------------------
+ * Bit-packed records (no upstream counterpart).  Upstream passes one int32 per
+ * syndrome bit / error entry (Examples/auxilary_functions.py:262-274), 32x the
+ * bytes the information needs; these entry points take each shot as LSB-first
+ * uint32 words instead (bit i of word k is entry 32k + i; bits past the last
+ * entry are ignored) and return the same results as the int32 calls.
+ *
+ * grand_decode_cc_packed: kind GRAND_PACKED_SYNDROMES gives ceil(n/32) syndrome
+ * words per shot, GRAND_PACKED_ERRORS ceil(m/32) error words (then is_equal and
+ * degeneracy are filled as with `errors`); probability_file NULL searches as
+ * grand_decode_cc, otherwise as grand_decode_prob_cc with that phase-mask file.
+ * grand_decode_cln_packed: ceil(n/32) detector words and ceil(n_logicos/32)
+ * logical words per shot; variant 0, 1, 2 searches as grand_decode_cln,
+ * grand_decode_prob_cln (file = phase masks) and grand_decode_ML_cln (file =
+ * LLRs).  Other arguments and return codes as the int32 calls. */
+#define GRAND_PACKED_SYNDROMES 0
+#define GRAND_PACKED_ERRORS 1
+int grand_decode_cc_packed(const int *Hx, const int *Hz, int n, int m, const unsigned int *records,
+                           int kind, int num_shots, const GrandDecoderConfig *config,
+                           GrandDecoderResult *results, char type_of_error,
+                           const char *probability_file);
+int grand_decode_cln_packed(const int *H_dem, const int *L_dem, int n, int m, int n_logicos,
+                            const unsigned int *detectors, const unsigned int *logicals,
+                            int num_shots, const GrandDecoderConfig *config,
+                            GrandDecoderResult *results, int variant, const char *file);
+
 const char *grand_version(void);
 const char *grand_last_error(void);
 

@@ -91,6 +91,14 @@ SIGNATURES = {
     "grand_decode_cc_noalloc": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
                                  ctypes.c_int, ctypes.POINTER(GrandDecoderConfig),
                                  ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "grand_decode_cc_packed": ([IP, IP, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
+                                ctypes.c_int, ctypes.POINTER(GrandDecoderConfig),
+                                ctypes.POINTER(GrandDecoderResult), ctypes.c_char, ctypes.c_char_p],
+                               ctypes.c_int),
+    "grand_decode_cln_packed": ([IP, IP, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                 ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(GrandDecoderConfig),
+                                 ctypes.POINTER(GrandDecoderResult), ctypes.c_int, ctypes.c_char_p],
+                                ctypes.c_int),
     "grand_version": ([], ctypes.c_char_p),
     "grand_last_error": ([], ctypes.c_char_p),
 }
@@ -230,3 +238,54 @@ def decode_dem_ex(lib, variant, H_dem, L_dem, detectors, logicals, cfg, file=Non
     else:
         rc = lib.grand_decode_cln_ex(*args, ctypes.byref(cfg), results, ctypes.byref(out))
     return rc, results_array(results), dec, dlog, cost
+
+
+PACKED_SYNDROMES, PACKED_ERRORS = 0, 1
+
+
+def pack_bits(rows) -> np.ndarray:
+    """(shots, entries) 0/1 array -> (shots, ceil(entries/32)) uint32 words, LSB-first:
+    bit i of word k is entry 32k + i (the layout of the *_packed entry points)."""
+    a = (np.asarray(rows) != 0).astype(np.uint8)
+    shots, n = a.shape
+    words = (n + 31) // 32
+    pad = np.zeros((shots, words * 32), dtype=np.uint8)
+    pad[:, :n] = a
+    b = np.packbits(pad.reshape(shots, words * 4, 8), axis=2, bitorder="little")
+    return np.ascontiguousarray(b.reshape(shots, words * 4)).view("<u4").reshape(shots, words)
+
+
+def _type_byte(error_type) -> bytes:
+    return error_type if isinstance(error_type, bytes) else str(error_type).encode()
+
+
+def decode_css_packed(lib, Hx, Hz, words, kind, cfg, error_type, prob_file=None):
+    """Bit-packed CSS records (pack_bits layout).  kind: PACKED_SYNDROMES or
+    PACKED_ERRORS; prob_file None searches as grand_decode_cc, otherwise as
+    grand_decode_prob_cc.  Returns (rc, results ndarray)."""
+    n_rows, n_cols = np.asarray(Hx).shape
+    hx, hz = _flat(Hx), _flat(Hz)
+    w = np.ascontiguousarray(words, dtype=np.uint32)
+    shots = w.shape[0]
+    results = (GrandDecoderResult * shots)()
+    rc = lib.grand_decode_cc_packed(_p(hx), _p(hz), n_rows, n_cols, w.ctypes.data, kind, shots,
+                                    ctypes.byref(cfg), results, ctypes.c_char(_type_byte(error_type)),
+                                    os.fsencode(prob_file) if prob_file else None)
+    return rc, results_array(results)
+
+
+def decode_dem_packed(lib, variant, H_dem, L_dem, det_words, log_words, cfg, file=None):
+    """Bit-packed DEM records (pack_bits layout); variant "uniform", "prob" or "ml".
+    Returns (rc, results ndarray)."""
+    n_rows, n_cols = np.asarray(H_dem).shape
+    nl = int(np.asarray(L_dem).shape[1])
+    h, l = _flat(H_dem), _flat(L_dem)
+    d = np.ascontiguousarray(det_words, dtype=np.uint32)
+    g = np.ascontiguousarray(log_words, dtype=np.uint32)
+    shots = d.shape[0]
+    results = (GrandDecoderResult * shots)()
+    v = {"uniform": 0, "prob": 1, "ml": 2}[variant]
+    rc = lib.grand_decode_cln_packed(_p(h), _p(l), n_rows, n_cols, nl, d.ctypes.data, g.ctypes.data,
+                                     shots, ctypes.byref(cfg), results, v,
+                                     os.fsencode(file) if file else None)
+    return rc, results_array(results)

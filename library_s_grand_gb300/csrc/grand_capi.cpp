@@ -170,7 +170,7 @@ struct WsGuard {
 int decode_css(int variant, const int *Hx, const int *Hz, int n, int m, const int *errors,
                const int *syndromes, int num_shots, const GrandDecoderConfig *config,
                GrandDecoderResult *results, char type_of_error, const char *pfile,
-               const GrandDecodeOutputs *out) {
+               const GrandDecodeOutputs *out, bool packed = false) {
   const int *H, *Ho;
   if (type_of_error == 'x' || type_of_error == 'X') {
     H = Hz;
@@ -239,6 +239,12 @@ int decode_css(int variant, const int *Hx, const int *Hz, int n, int m, const in
   req.codes.push_back(make_devcode(*tab, p));
   req.h_in = errors ? errors : syndromes;
   req.in_ints = (size_t)num_shots * (errors ? m : n);
+  if (packed) {  // ceil(m/32) error words or ceil(n/32) syndrome words per shot
+    const int words = errors ? (m + 31) / 32 : (n + 31) / 32;
+    req.in_ints = (size_t)num_shots * words;
+    req.codes[0].rec_len = words;
+    req.codes[0].packed = 1;
+  }
   req.h_results = results;
   req.h_dec_err = out ? out->decoded_errors : nullptr;
   req.dec_m = m;
@@ -250,7 +256,8 @@ int decode_css(int variant, const int *Hx, const int *Hz, int n, int m, const in
 
 int decode_dem(int variant, const int *H, const int *L, int n, int m, int nl, const int *det,
                const int *logicals, int num_shots, const GrandDecoderConfig *config,
-               GrandDecoderResult *results, const char *file, const GrandDecodeOutputs *out) {
+               GrandDecoderResult *results, const char *file, const GrandDecodeOutputs *out,
+               bool packed = false) {
   if (!config) {
     fprintf(stderr, "grand: config is NULL\n");
     return GRAND_ERR_INVALID;
@@ -318,6 +325,12 @@ int decode_dem(int variant, const int *H, const int *L, int n, int m, int nl, co
   static const int zero = 0;
   req.h_in_log = nl > 0 ? logicals : &zero;
   req.in_log_ints = nl > 0 ? (size_t)num_shots * nl : 1;
+  if (packed) {  // ceil(n/32) detector words and ceil(nl/32) logical words per shot
+    req.in_ints = (size_t)num_shots * ((n + 31) / 32);
+    req.in_log_ints = nl > 0 ? (size_t)num_shots * ((nl + 31) / 32) : 1;
+    req.codes[0].rec_len = (n + 31) / 32;
+    req.codes[0].packed = 1;
+  }
   req.h_results = results;
   req.h_dec_err = out ? out->decoded_errors : nullptr;
   req.h_dec_log = out ? out->decoded_logicals : nullptr;
@@ -415,6 +428,34 @@ int grand_decode_ML_cln_ex(int *H_dem, const int *L_dem, int n, int m, int n_log
                            const char *llr_file, const GrandDecodeOutputs *out) {
   return decode_dem(kMl, H_dem, L_dem, n, m, n_logicos, detectors, logicals, num_shots, config,
                     results, llr_file, out);
+}
+
+int grand_decode_cc_packed(const int *Hx, const int *Hz, int n, int m, const unsigned int *records,
+                           int kind, int num_shots, const GrandDecoderConfig *config,
+                           GrandDecoderResult *results, char type_of_error,
+                           const char *probability_file) {
+  if (kind != GRAND_PACKED_SYNDROMES && kind != GRAND_PACKED_ERRORS) {
+    fprintf(stderr, "grand: packed record kind %d is neither syndromes (0) nor errors (1)\n", kind);
+    return GRAND_ERR_INVALID;
+  }
+  const int *rec = reinterpret_cast<const int *>(records);
+  return decode_css(probability_file ? kProb : kUniform, Hx, Hz, n, m,
+                    kind == GRAND_PACKED_ERRORS ? rec : nullptr,
+                    kind == GRAND_PACKED_SYNDROMES ? rec : nullptr, num_shots, config, results,
+                    type_of_error, probability_file, nullptr, true);
+}
+
+int grand_decode_cln_packed(const int *H_dem, const int *L_dem, int n, int m, int n_logicos,
+                            const unsigned int *detectors, const unsigned int *logicals,
+                            int num_shots, const GrandDecoderConfig *config,
+                            GrandDecoderResult *results, int variant, const char *file) {
+  if (variant < kUniform || variant > kMl) {
+    fprintf(stderr, "grand: DEM variant %d is not uniform (0), prob (1) or ML (2)\n", variant);
+    return GRAND_ERR_INVALID;
+  }
+  return decode_dem(variant, H_dem, L_dem, n, m, n_logicos, reinterpret_cast<const int *>(detectors),
+                    reinterpret_cast<const int *>(logicals), num_shots, config, results, file,
+                    nullptr, true);
 }
 
 const char *grand_version(void) { return "grand-gb300 0.1 (sm_103a)"; }

@@ -77,7 +77,10 @@ struct DevCode {
   int mask_order[kMaxMasks][3];
   int n_logicos, nlw;
   int rank;                  // rank of RREF(H_other), CSS
-  int rec_len;               // int32 entries per shot record
+  int rec_len;               // int32 entries (or packed words) per shot record
+  int packed;                // 1: records are bit-packed uint32 words (bit i of word k =
+                             // entry 32k + i): ceil(R/32) syndrome / detector words (then
+                             // ceil(n_logicos/32) logical words for DEM), ceil(m/32) error words
   const uint32_t *cols;      // m * nwp
   const int *colw;           // m
   const uint32_t *rows;      // R * mw (CSS, errors input)

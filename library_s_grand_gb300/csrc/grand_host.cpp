@@ -337,6 +337,7 @@ DevCode make_devcode(const CodeTables &t, const CallParams &p) {
   d.nlw = t.nlw;
   d.rank = t.rank;
   d.rec_len = p.rec_len ? p.rec_len : (p.input_kind == kInErrors ? t.m : t.R);
+  d.packed = p.packed;
   d.cols = t.cols;
   d.colw = t.colw;
   d.rows = nullptr;

@@ -49,6 +49,7 @@ struct CallParams {
   int mask_order[kMaxMasks][3] = {};
   const float *d_llr = nullptr;   // device LLRs (ML)
   int rec_len = 0;                 // int32 entries per record (0: R, or m for errors)
+  int packed = 0;                  // records are bit-packed words (rec_len then counts words)
 };
 
 DevCode make_devcode(const CodeTables &t, const CallParams &p);

@@ -478,7 +478,44 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
     // ---- pack the record ---------------------------------------------------
     uint32_t s_lane = 0;  // lane w holds syndrome word w
     int original_weight = 0;
-    if (cd.input_kind == kInErrors) {
+    if (cd.packed) {
+      // bit-packed records: the words are the bits (bits past the last entry ignored)
+      const int nwords = cd.input_kind == kInErrors ? cd.mw : cd.nw;
+      const int nbits = cd.input_kind == kInErrors ? cd.m : cd.R;
+      uint32_t *dst = cd.input_kind == kInErrors ? A.eb : A.sw;
+      for (int q = lane; q < nwords; q += 32) {
+        uint32_t v = __ldg(reinterpret_cast<const uint32_t *>(rec) + q);
+        if (q == nwords - 1 && (nbits & 31)) v &= (1u << (nbits & 31)) - 1u;
+        dst[q] = v;
+        original_weight += __popc(v);
+      }
+      if (cd.family == kDem) {
+        const uint32_t *lg = b.in_log ? reinterpret_cast<const uint32_t *>(b.in_log) + (size_t)shot * cd.nlw
+                                      : reinterpret_cast<const uint32_t *>(rec) + cd.nw;
+        for (int q = lane; q < cd.nlw; q += 32) {
+          uint32_t v = __ldg(lg + q);
+          if (q == cd.nlw - 1 && (cd.n_logicos & 31)) v &= (1u << (cd.n_logicos & 31)) - 1u;
+          A.eb[q] = v;
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) original_weight += __shfl_xor_sync(kFull, original_weight, o);
+      if (cd.input_kind != kInErrors) original_weight = 0;
+      prefetch_next_record(b, __shfl_sync(kFull, (int)nxt, 0));
+      __syncwarp();
+      if (cd.input_kind == kInErrors) {
+        for (int q = 0; q < cd.mw; ++q) {
+          uint32_t word = A.eb[q];
+          while (word) {
+            const int c = q * 32 + __ffs(word) - 1;
+            word &= word - 1u;
+            if (lane < cd.nw) s_lane ^= __ldg(cd.cols + (size_t)c * cd.nwp + lane);
+          }
+        }
+      } else {
+        s_lane = lane < cd.nw ? A.sw[lane] : 0u;
+      }
+    } else if (cd.input_kind == kInErrors) {
       original_weight = pack_ballots(rec, cd.m, A.eb);
       prefetch_next_record(b, __shfl_sync(kFull, (int)nxt, 0));
       __syncwarp();

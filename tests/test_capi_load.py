@@ -136,3 +136,20 @@ def test_zero_shots_returns_zero_without_gpu(lib):
 
 def test_version_string(lib):
     assert b"sm_103a" in lib.grand_version()
+
+
+def test_packed_kind_rejected_without_gpu(lib, capfd):
+    c = S.BB_CODES[72]()
+    words = np.zeros((2, 2), dtype=np.uint32)
+    rc, _ = capi.decode_css_packed(lib, c.hx, c.hz, words, 7, _cfg(3), b"x")
+    assert rc == -1
+    assert "packed record kind" in capfd.readouterr().err
+
+
+def test_pack_bits_layout():
+    a = (np.random.default_rng(0).random((6, 70)) < 0.3).astype(np.int32)
+    w = capi.pack_bits(a)
+    assert w.shape == (6, 3) and w.dtype == np.uint32
+    for i in range(6):
+        for j in range(70):
+            assert (int(w[i, j // 32]) >> (j % 32)) & 1 == a[i, j]
