@@ -50,6 +50,19 @@ int grand_engine_add_dem(GrandEngine *engine, const int *H_dem, const int *L_dem
 /* int32 entries per shot record of a registered code (or < 0). */
 int grand_engine_record_len(GrandEngine *engine, int code_id);
 
+/* On-device shot generation (no upstream counterpart; upstream draws shots in
+ * Python).  Draws num_shots shots of code `code_id`: every error position (CSS:
+ * qubit, DEM: mechanism) flips independently with probability d_p[j] (m FP32
+ * values in device memory), and the code's records (grand_engine_record_len
+ * ints per shot: errors or syndrome for CSS as registered, detectors then true
+ * logical flips for DEM) are written to d_records, ready for
+ * grand_engine_decode_device.  The draws come from Philox4x32-10 keyed by
+ * `seed`; shot first_shot + i always gets the same draws, whatever the batch
+ * split.  Asynchronous on `stream`. */
+int grand_engine_sample(GrandEngine *engine, int code_id, const float *d_p,
+                        unsigned long long seed, unsigned long long first_shot, int num_shots,
+                        int *d_records, void *stream);
+
 /* Decode num_shots records, concatenated in shot order, from host memory.
  * shot_code may be NULL when every shot uses code 0.  Synchronous. */
 int grand_engine_decode(GrandEngine *engine, int num_shots, const int *shot_code,

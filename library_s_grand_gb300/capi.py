@@ -259,6 +259,20 @@ def _type_byte(error_type) -> bytes:
     return error_type if isinstance(error_type, bytes) else str(error_type).encode()
 
 
+def run_grand_shots_cc_packed(lib, Hx, Hz, words, kind, cfg, error_type, prob_file=None):
+    """Bit-packed CSS records in the style of the run_grand_* helpers: returns
+    (rc, ctypes GrandDecoderResult array) without converting the results."""
+    n_rows, n_cols = np.asarray(Hx).shape
+    hx, hz = _flat(Hx), _flat(Hz)
+    w = np.ascontiguousarray(words, dtype=np.uint32)
+    shots = w.shape[0]
+    results = (GrandDecoderResult * shots)()
+    rc = lib.grand_decode_cc_packed(_p(hx), _p(hz), n_rows, n_cols, w.ctypes.data, kind, shots,
+                                    ctypes.byref(cfg), results, ctypes.c_char(_type_byte(error_type)),
+                                    os.fsencode(prob_file) if prob_file else None)
+    return rc, results
+
+
 def decode_css_packed(lib, Hx, Hz, words, kind, cfg, error_type, prob_file=None):
     """Bit-packed CSS records (pack_bits layout).  kind: PACKED_SYNDROMES or
     PACKED_ERRORS; prob_file None searches as grand_decode_cc, otherwise as

@@ -127,6 +127,25 @@ int grand_engine_add_dem(GrandEngine *e, const int *H, const int *L, int n, int 
   return 0;
 }
 
+int grand_engine_sample(GrandEngine *e, int code_id, const float *d_p, unsigned long long seed,
+                        unsigned long long first_shot, int num_shots, int *d_records,
+                        void *stream) {
+  if (!e || num_shots < 0 || !d_p || (num_shots > 0 && !d_records)) return GRAND_ERR_INVALID;
+  DevCode cd;
+  {
+    std::lock_guard<std::mutex> lk(e->mu);
+    if (code_id < 0 || code_id >= (int)e->codes.size()) return GRAND_ERR_INVALID;
+    cd = e->codes[code_id];
+  }
+  cudaError_t r = launch_sample(cd, d_p, seed, first_shot, num_shots, d_records,
+                                e->ctx->sm_count, (cudaStream_t)stream);
+  if (r != cudaSuccess) {
+    set_error("grand_engine_sample: %s", cudaGetErrorString(r));
+    return GRAND_ERR_CUDA;
+  }
+  return 0;
+}
+
 int grand_engine_record_len(GrandEngine *e, int code_id) {
   if (!e || code_id < 0 || code_id >= (int)e->rec_len.size()) return GRAND_ERR_INVALID;
   return e->rec_len[code_id];

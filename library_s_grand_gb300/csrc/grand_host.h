@@ -16,6 +16,9 @@ namespace grand {
 cudaError_t launch_triage(const DevBatch &b, int grid, cudaStream_t s);
 cudaError_t launch_search(const DevBatch &b, int grid, cudaStream_t s);
 cudaError_t triage_occupancy(int *blocks_per_sm);
+cudaError_t launch_sample(const DevCode &cd, const float *d_p, unsigned long long seed,
+                          unsigned long long first_shot, int num_shots, int *d_records,
+                          int sm_count, cudaStream_t s);  // grand_sample.cu
 cudaError_t occupancy(int *triage_blocks_per_sm, int *search_blocks_per_sm);
 
 void set_error(const char *fmt, ...);

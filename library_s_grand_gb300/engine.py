@@ -31,6 +31,8 @@ _SIGS = {
     "grand_engine_kernel_times": ([VP, VP, ctypes.POINTER(ctypes.c_float),
                                    ctypes.POINTER(ctypes.c_float)], ctypes.c_int),
     "grand_engine_batch_times": ([VP] + [ctypes.POINTER(ctypes.c_float)] * 4, ctypes.c_int),
+    "grand_engine_sample": ([VP, ctypes.c_int, VP, ctypes.c_ulonglong, ctypes.c_ulonglong,
+                             ctypes.c_int, VP, VP], ctypes.c_int),
     "grand_measure_int_peak": ([], ctypes.c_double),
     "grand_device_info": ([ctypes.c_char_p, ctypes.c_int], ctypes.c_int),
 }
@@ -144,6 +146,12 @@ class Engine:
         a, b = ctypes.c_float(), ctypes.c_float()
         rc = self.lib.grand_engine_kernel_times(self.h, stream or None, ctypes.byref(a), ctypes.byref(b))
         return (a.value, b.value) if rc == 0 else (None, None)
+
+    def sample(self, code_id, d_p, seed, first_shot, num_shots, d_records, stream=0):
+        """Draw shots of a registered code on the device (device pointers d_p: m FP32
+        flip probabilities, d_records: num_shots * record_len int32)."""
+        return self.lib.grand_engine_sample(self.h, code_id, d_p, seed, first_shot, num_shots,
+                                            d_records, stream or None)
 
     def batch_times(self):
         """(h2d, triage, search, d2h) ms of the last host-buffer decode."""
