@@ -79,23 +79,6 @@ __device__ __forceinline__ void colex_unrank(const unsigned long long *t, unsign
   }
 }
 
-// Lexicographic unranking (upstream order): rank -> ascending c[0..w-1] of [0, n).
-// Computed through the colex rank of the reflected subset {n-1-c}.
-__device__ __forceinline__ void lex_unrank(const unsigned long long *t, unsigned long long rank,
-                                           int n, int w, int (&c)[kMaxW]) {
-  unsigned long long q = ncr(t, n, w) - 1ull - rank;
-  int hi = n - 1;
-#pragma unroll
-  for (int i = kMaxW; i >= 1; --i) {
-    if (i <= w) {
-      int v = ncr_floor(t, q, i, i - 1, hi);
-      q -= ncr(t, v, i);
-      c[w - i] = n - 1 - v;
-      hi = v - 1;
-    }
-  }
-}
-
 // Largest i in [lo, hi] with key(i) <= x, for key non-decreasing and
 // key(lo) <= x.  Each step the 32 lanes probe 32 points of the range, so n
 // entries take ceil(log32 n) dependent loads instead of log2 n.
@@ -113,10 +96,12 @@ __device__ __forceinline__ int warp_search_le(int lo, int hi, unsigned long long
   return lo;
 }
 
-// lex_unrank with the whole warp: each element's binomial search probes 32
-// points per step (warp_search_le) and computes the binomials instead of
-// loading them, so a result writer's unranking is a few rounds of ballots with
-// no dependent memory loads.  Every lane gets c.
+// Lexicographic unranking (upstream order): rank -> ascending c[0..w-1] of
+// [0, n), through the colex rank of the reflected subset {n-1-c}, by the whole
+// warp: each element's binomial search probes 32 points per step
+// (warp_search_le) and computes the binomials instead of loading them, so a
+// result writer's unranking is a few rounds of ballots with no dependent memory
+// loads.  Every lane gets c.
 __device__ __forceinline__ void lex_unrank_warp(unsigned long long rank, int n, int w,
                                                 int (&c)[kMaxW]) {
   unsigned long long q = binom(n, w) - 1ull - rank;
