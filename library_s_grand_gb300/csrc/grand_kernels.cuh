@@ -1,7 +1,7 @@
 // grand_kernels.cuh -- what the triage and search kernels share: launch
-// constants, the per-shot result writer and the first-hit winner lookup.  The two kernels live in their
-// own translation units (grand_triage.cu, grand_search.cu) so they compile in
-// parallel.
+// constants, the per-shot result writer and the first-hit winner lookup.  The
+// two kernels live in their own translation units (grand_triage.cu,
+// grand_search.cu) so they compile in parallel.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -10,13 +10,13 @@
 
 namespace grand {
 
-constexpr int kTriageWarps = 4;
-constexpr int kLightTam = 96;
-constexpr int kLightWords = kLightTam * 8;
+constexpr int kTriageWarps = 4;                 // warps per triage block
+constexpr int kLightTam = 96;                   // largest active set the triage warp searches
+constexpr int kLightWords = kLightTam * 8;      // its staged column words (nwp <= 8)
 constexpr int kSearchThreads = 256;
 constexpr int kSearchWarps = kSearchThreads / 32;
-constexpr int kWarpStage = 1280;  // staged active-column words per search warp
-constexpr int kTilesPerFetch = 4;
+constexpr int kWarpStage = 1280;  // per search warp: staged column sketches, or the Job at its end
+constexpr int kTilesPerFetch = 4;  // most tiles a search warp draws at once
 constexpr int kRunKK = 8;       // prefixes per lane in a run tile (search kernel)
 constexpr int kRunKKLight = 4;  // the same inside the triage warp's light search
 

@@ -3,7 +3,7 @@
 // search_kernel (persistent, every warp an independent worker)
 //   every warp repeatedly takes the next tiles (K colex prefixes per lane of
 //   one weight block of one Job) from a global counter, stages the iteration's
-//   active columns in its own shared-memory slice, evaluates them, publishes
+//   column sketches in its own shared-memory slice, evaluates them, publishes
 //   the lowest matching global index (atomicMin) or the lowest {cost, rank}
 //   key (128-bit CAS), and the warp that completes a Job's last tile writes its
 //   result.  Tiles whose candidates all rank above an already-found match are
