@@ -175,7 +175,8 @@ struct DevBatch {
   unsigned *status;
   int *deferred;                 // per shot: 1 if the shot must be re-run
   int light_max_log2;            // light-path budget (candidates, log2)
-  int tile_k;                    // prefixes per lane per tile for weights >= 3
+  int tile_k;                    // prefixes per lane per colex tile (weights <= 2)
+  int has_ml;                    // some code of the batch is ML: launch the kernels' ML builds
 };
 
 }  // namespace grand

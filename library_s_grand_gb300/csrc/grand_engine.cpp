@@ -265,6 +265,7 @@ int grand_engine_decode_device(GrandEngine *e, int num_shots, const int *d_shot_
   b.deferred = (int *)slot->d_deferred;
   b.light_max_log2 = e->tn.light_max_log2;
   b.tile_k = e->tn.tile_k;
+  for (const DevCode &c : e->codes) b.has_ml |= c.variant == kMl;
   if (!use_graph) {
     cudaEventRecord(slot->ev[0], s);
     r = launch_pipeline(e->ctx, b, e->tn, s, slot->ev[1]);

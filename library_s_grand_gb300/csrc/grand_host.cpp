@@ -463,6 +463,7 @@ int run_batch(Context *ctx, Workspace *ws, const BatchRequest &req, BatchTiming 
   b.deferred = (int *)ws->d_deferred;
   b.light_max_log2 = tn.light_max_log2;
   b.tile_k = tn.tile_k;
+  for (const DevCode &c : req.codes) b.has_ml |= c.variant == kMl;
 
   std::vector<int> map;
   int todo = N;

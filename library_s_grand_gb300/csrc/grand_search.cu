@@ -69,6 +69,8 @@ __device__ Winner winner_ml(const Job &J) {
   return wn;
 }
 
+// MLK = false: a build without the ML paths for batches without ML codes.
+template <bool MLK>
 __global__ void __launch_bounds__(kSearchThreads, 3) search_kernel(DevBatch b) {
   __shared__ __align__(16) uint32_t s_stage[kSearchWarps][kWarpStage];
   __shared__ uint32_t s_sw[kSearchWarps][kMaxRows / 32];
@@ -152,7 +154,7 @@ __global__ void __launch_bounds__(kSearchThreads, 3) search_kernel(DevBatch b) {
         s_runs = S.runs;
         s_cum = S.cum;
         s_iter = S.iter;
-        s_ml = cdp->variant == kMl;
+        s_ml = MLK && cdp->variant == kMl;
         s_prob = cdp->variant == kProb;
         // the scans read only the column sketches: those are staged (the full
         // columns are read from the Job's scratch for the rare exact tests)
@@ -258,7 +260,8 @@ __global__ void __launch_bounds__(kSearchThreads, 3) search_kernel(DevBatch b) {
 // Host-callable launcher.
 // ---------------------------------------------------------------------------
 cudaError_t launch_search(const DevBatch &b, int grid, cudaStream_t s) {
-  search_kernel<<<grid, kSearchThreads, 0, s>>>(b);
+  if (b.has_ml) search_kernel<true><<<grid, kSearchThreads, 0, s>>>(b);
+  else search_kernel<false><<<grid, kSearchThreads, 0, s>>>(b);
   return cudaGetLastError();
 }
 
@@ -267,7 +270,7 @@ int search_threads_per_block() { return kSearchThreads; }
 cudaError_t occupancy(int *triage_blocks_per_sm, int *search_blocks_per_sm) {
   cudaError_t e = triage_occupancy(triage_blocks_per_sm);
   if (e != cudaSuccess) return e;
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(search_blocks_per_sm, search_kernel,
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(search_blocks_per_sm, search_kernel<true>,
                                                        kSearchThreads, 0);
 }
 

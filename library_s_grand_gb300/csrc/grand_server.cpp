@@ -150,6 +150,7 @@ cudaError_t start_slot(GrandServer *S, SrvSlot *sl) {
   b.deferred = sl->d_deferred;
   b.light_max_log2 = e->tn.light_max_log2;
   b.tile_k = e->tn.tile_k;
+  for (const DevCode &c : e->codes) b.has_ml |= c.variant == kMl;
   if (err == cudaSuccess) err = launch_pipeline(e->ctx, b, e->tn, s);
   if (err == cudaSuccess)
     err = cudaMemcpyAsync(sl->h_res, sl->d_res, sizeof(GrandDecoderResult) * shot,

@@ -121,10 +121,11 @@ __device__ int plan_next(const DevCode &cd, int tam0, int tam1, int tam2, int L,
 // ---------------------------------------------------------------------------
 // Staging of one iteration's active set (positions, columns, sketches, LLRs).
 // ---------------------------------------------------------------------------
+template <bool MLK>
 __device__ void stage_iteration(const DevCode &cd, const uint32_t *am, int tam, int *pos,
                                 int *tmp, uint32_t *cols, uint32_t *hcols, float *llr) {
   const int lane = threadIdx.x & 31;
-  const bool ml = cd.variant == kMl;
+  const bool ml = MLK && cd.variant == kMl;
   int *dst = ml ? tmp : pos;
   // ascending column indices of the first tam set bits (upstream extract_positions)
   int base = 0;
@@ -341,12 +342,13 @@ __device__ void small_iteration(const uint32_t *cols, const uint32_t *hcols, con
 // ---------------------------------------------------------------------------
 // Kernel 1: triage + light search.
 // ---------------------------------------------------------------------------
+template <bool MLK>
 __device__ void light_search(const DevBatch &b, const DevCode &cd, Job &J, WarpArea &A, int ii,
                              Winner &wn) {
   const int lane = threadIdx.x & 31;
-  const bool ml = cd.variant == kMl;
+  const bool ml = MLK && cd.variant == kMl;
   IterInfo &I = J.it[ii];
-  stage_iteration(cd, A.am[I.src], I.tam, A.pos, A.tmp, A.cols, A.hcols, A.llr);
+  stage_iteration<MLK>(cd, A.am[I.src], I.tam, A.pos, A.tmp, A.cols, A.hcols, A.llr);
   if (lane == 0) {
     I.pos = A.pos;
     I.cols = A.cols;
@@ -454,6 +456,8 @@ __device__ void light_search(const DevBatch &b, const DevCode &cd, Job &J, WarpA
   }
 }
 
+// MLK = false: a build without the ML paths (smaller code) for batches without ML codes.
+template <bool MLK>
 __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
   __shared__ WarpArea areas[kTriageWarps];
   const int lane = threadIdx.x & 31;
@@ -612,7 +616,7 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
 
     // ---- iterations in upstream order; the first one over the light budget
     //      and everything after it go to the search kernel ---------------------
-    const bool ml = cd.variant == kMl;
+    const bool ml = MLK && cd.variant == kMl;
     const unsigned long long budget = 1ull << b.light_max_log2;
     Winner wn;
     wn.found = 0;
@@ -637,7 +641,7 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
         __syncwarp();
         break;
       }
-      light_search(b, cd, J, A, ii, wn);
+      light_search<MLK>(b, cd, J, A, ii, wn);
       if (wn.found) break;
     }
     if (heavy_from < 0) {
@@ -694,7 +698,7 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
         llr = reinterpret_cast<float *>(sp);
         sp += (tm + 3ull) & ~3ull;
       }
-      stage_iteration(cd, A.am[I.src], I.tam, pos, tmp, cols, hcols, llr);
+      stage_iteration<MLK>(cd, A.am[I.src], I.tam, pos, tmp, cols, hcols, llr);
       if (lane == 0) {
         I.pos = pos;
         I.cols = cols;
@@ -786,14 +790,15 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
 // Host-callable launcher.
 // ---------------------------------------------------------------------------
 cudaError_t launch_triage(const DevBatch &b, int grid, cudaStream_t s) {
-  triage_kernel<<<grid, kTriageWarps * 32, 0, s>>>(b);
+  if (b.has_ml) triage_kernel<true><<<grid, kTriageWarps * 32, 0, s>>>(b);
+  else triage_kernel<false><<<grid, kTriageWarps * 32, 0, s>>>(b);
   return cudaGetLastError();
 }
 
 int triage_warps_per_block() { return kTriageWarps; }
 
 cudaError_t triage_occupancy(int *blocks_per_sm) {
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, triage_kernel,
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, triage_kernel<true>,
                                                        kTriageWarps * 32, 0);
 }
 
