@@ -380,7 +380,7 @@ def run_ours(args):
 
 # DRAM bytes (read + write) of one triage_kernel launch on the headline batch, from an ncu
 # --set full capture of `bench.py --case headline`.
-TRIAGE_TRAFFIC = 9.591552e6 + 26.368e3
+TRIAGE_TRAFFIC = 9.541120e6 + 0.0
 
 
 def hbm_peak():
@@ -410,7 +410,7 @@ STRESS_SHOTS = 192
 SKETCH_OPS_PER_CANDIDATE = 1.5
 # DRAM bytes (read + write) of one search_kernel launch on the stress input, from an ncu
 # --set full capture of `bench.py --case stress` (48 shots), scaled to 192 shots.
-STRESS_TRAFFIC_PER_SHOT = (1.019136e6 + 47.36e3) / 48
+STRESS_TRAFFIC_PER_SHOT = (1.940992e6 + 6.144e3) / 48
 
 
 def stress_case(torch, lib, dev, n=STRESS_SHOTS):
