@@ -83,8 +83,11 @@ __device__ int plan_next(const DevCode &cd, int tam0, int tam1, int tam2, int L,
       S.runs = w >= 3 ? 1 : 0;
       S.cum = nullptr;
       S.K = S.runs ? kRunKK : tile_k;
-      // run-tile counts are built by the warp when a Job is published
-      S.ntiles = S.runs ? 0ull : (S.nprefix + 32ull * S.K - 1) / (32ull * S.K);
+      // run-tile counts are built by the warp when a Job is published; colex
+      // blocks (w <= 2) have at most tam - 1 prefixes, so 32-bit division does
+      S.ntiles = S.runs ? 0ull
+                        : (unsigned long long)(((unsigned)S.nprefix + 32u * (unsigned)S.K - 1u) /
+                                               (32u * (unsigned)S.K));
       tot += S.count;
       if (cd.variant == kProb) I.phase_end[k] = tot;
     };
@@ -192,7 +195,7 @@ __device__ __forceinline__ int pack_ballots(const int *p, int n, uint32_t *dst) 
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
       const int i = (q0 + u) * 32 + lane;
-      v[u] = i < n ? p[i] : 0;
+      v[u] = i < n ? __ldcg(p + i) : 0;  // read once: kept out of L1
     }
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
@@ -342,6 +345,47 @@ __device__ void small_iteration(const uint32_t *cols, const uint32_t *hcols, con
 // ---------------------------------------------------------------------------
 // Kernel 1: triage + light search.
 // ---------------------------------------------------------------------------
+// First-hit search of an iteration with one active position (most shots at low
+// error rates): its only candidate is that column, weight 1, rank 0 of the
+// first weight-1 block, and it matches when the column equals the syndrome.
+// The same winner as the small-set path, without staging the iteration.
+__device__ void single_search(const DevCode &cd, Job &J, WarpArea &A, int ii, Winner &wn) {
+  const int lane = threadIdx.x & 31;
+  IterInfo &I = J.it[ii];
+  int s = I.seg_lo;
+  while (s < I.seg_hi && (J.seg[s].w != 1 || J.seg[s].dup)) ++s;
+  if (s >= I.seg_hi) return;  // no weight-1 block: nothing to search
+  // the active position: the lowest set bit of the iteration's threshold mask
+  const uint32_t *am = A.am[I.src];
+  int pos = -1;
+  for (int q0 = 0; q0 < cd.mw && pos < 0; q0 += 32) {
+    const uint32_t word = q0 + lane < cd.mw ? am[q0 + lane] : 0u;
+    const unsigned nz = __ballot_sync(kFull, word != 0u);
+    if (nz) {
+      const int l = __ffs(nz) - 1;
+      pos = (q0 + l) * 32 + __ffs(__shfl_sync(kFull, word, l)) - 1;
+    }
+  }
+  if (pos < 0) return;
+  const bool eq = lane >= cd.nw || __ldg(cd.cols + (size_t)pos * cd.nwp + lane) == A.sw[lane];
+  if (!__all_sync(kFull, eq)) return;
+  const Seg &S = J.seg[s];
+  wn.found = 1;
+  wn.ii = ii;
+  wn.seg = s;
+  wn.rank = 0;
+  wn.count = I.branch == kBranchCpu ? S.base - I.base + 1ull             // grand_decoder.cu:547-548
+             : cd.variant == kProb  ? I.phase_end[S.phase]              // grand_decoder.cu:1006
+                                    : I.total;                          // grand_decoder.cu:1303-1304
+  wn.cost = 0.0f;
+  wn.mask = 1u;  // position 0 of the iteration's list
+  if (lane == 0) {
+    A.pos[0] = pos;
+    I.pos = A.pos;
+  }
+  __syncwarp();
+}
+
 template <bool MLK>
 __device__ void light_search(const DevBatch &b, const DevCode &cd, Job &J, WarpArea &A, int ii,
                              Winner &wn) {
@@ -488,7 +532,7 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
       const int nbits = cd.input_kind == kInErrors ? cd.m : cd.R;
       uint32_t *dst = cd.input_kind == kInErrors ? A.eb : A.sw;
       for (int q = lane; q < nwords; q += 32) {
-        uint32_t v = __ldg(reinterpret_cast<const uint32_t *>(rec) + q);
+        uint32_t v = __ldcg(reinterpret_cast<const uint32_t *>(rec) + q);
         if (q == nwords - 1 && (nbits & 31)) v &= (1u << (nbits & 31)) - 1u;
         dst[q] = v;
         original_weight += __popc(v);
@@ -497,7 +541,7 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
         const uint32_t *lg = b.in_log ? reinterpret_cast<const uint32_t *>(b.in_log) + (size_t)shot * cd.nlw
                                       : reinterpret_cast<const uint32_t *>(rec) + cd.nw;
         for (int q = lane; q < cd.nlw; q += 32) {
-          uint32_t v = __ldg(lg + q);
+          uint32_t v = __ldcg(lg + q);
           if (q == cd.nlw - 1 && (cd.n_logicos & 31)) v &= (1u << (cd.n_logicos & 31)) - 1u;
           A.eb[q] = v;
         }
@@ -572,23 +616,55 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
 
     // ---- flagged-check counts and threshold masks ---------------------------
     const int L = cd.max_soma < kMaxIters ? cd.max_soma : kMaxIters;
+    // Four mask words (128 columns) per pass, with every column load of the
+    // pass issued before the first use: one memory round trip per 128 columns.
     int tam_raw[3] = {0, 0, 0};
-    for (int q = 0; q < cd.mw; ++q) {
-      const int c = q * 32 + lane;
-      int sum = 0;
-      if (c < cd.m) {
-        const uint32_t *col = cd.cols + (size_t)c * cd.nwp;
-        for (int k = 0; k < cd.nw; ++k) sum += __popc(__ldg(col + k) & A.sw[k]);
-        if (!cd.regular) {
-          const int cw = __ldg(cd.colw + c);
-          sum = cw == 0 ? 0 : sum + (cd.max_soma - cw);
+    for (int q0 = 0; q0 < cd.mw; q0 += 4) {
+      int sum[4] = {0, 0, 0, 0};
+      if (cd.nwp == 4) {  // R <= 128: a column is one 16-byte word group
+        uint4 v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int c = (q0 + u) * 32 + lane;
+          v[u] = c < cd.m ? __ldg(reinterpret_cast<const uint4 *>(cd.cols) + c)
+                          : make_uint4(0u, 0u, 0u, 0u);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)  // words past nw meet zero syndrome words
+          sum[u] = __popc(v[u].x & A.sw[0]) + __popc(v[u].y & A.sw[1]) +
+                   __popc(v[u].z & A.sw[2]) + __popc(v[u].w & A.sw[3]);
+      } else {
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int c = (q0 + u) * 32 + lane;
+          if (c < cd.m) {
+            const uint32_t *col = cd.cols + (size_t)c * cd.nwp;
+            for (int k = 0; k < cd.nw; ++k) sum[u] += __popc(__ldg(col + k) & A.sw[k]);
+          }
         }
       }
+      if (!cd.regular) {
+        int cw[4];
 #pragma unroll
-      for (int i = 0; i < kMaxIters; ++i) {
-        const uint32_t bits = __ballot_sync(kFull, c < cd.m && i < L && sum >= cd.max_soma - i);
-        if (lane == 0) A.am[i][q] = bits;
-        tam_raw[i] += __popc(bits);
+        for (int u = 0; u < 4; ++u) {
+          const int c = (q0 + u) * 32 + lane;
+          cw[u] = c < cd.m ? __ldg(cd.colw + c) : 0;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) sum[u] = cw[u] == 0 ? 0 : sum[u] + (cd.max_soma - cw[u]);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int q = q0 + u;
+        if (q >= cd.mw) break;
+        const int c = q * 32 + lane;
+#pragma unroll
+        for (int i = 0; i < kMaxIters; ++i) {
+          const uint32_t bits =
+              __ballot_sync(kFull, c < cd.m && i < L && sum[u] >= cd.max_soma - i);
+          if (lane == 0) A.am[i][q] = bits;
+          tam_raw[i] += __popc(bits);
+        }
       }
     }
     __shared__ PlanState plans[kTriageWarps];
@@ -641,7 +717,8 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
         __syncwarp();
         break;
       }
-      light_search<MLK>(b, cd, J, A, ii, wn);
+      if (!ml && I.tam == 1) single_search(cd, J, A, ii, wn);
+      else light_search<MLK>(b, cd, J, A, ii, wn);
       if (wn.found) break;
     }
     if (heavy_from < 0) {
