@@ -170,20 +170,21 @@ static __device__ void finish_shot(const DevBatch &b, const DevCode &cd, const J
                                 : lane < 16 ? 0ull
                                             : (wn.found ? now - J.t_start : 0ull);
   const unsigned long long dbits = (unsigned long long)__double_as_longlong(1e-6 * (double)dt);
-  uint32_t v = 0;
-  switch (lane) {
-    case 0: v = (uint32_t)wn.found; break;
-    case 1: v = (uint32_t)w; break;
-    case 2: v = (uint32_t)J.original_weight; break;
-    case 3: v = (uint32_t)degenerate; break;
-    case 4: v = (uint32_t)is_equal; break;
-    case 5: v = (uint32_t)(wn.found ? J.it[wn.ii].tam : J.final_tam); break;
-    case 6: v = (uint32_t)tested; break;
-    case 7: v = (uint32_t)(tested >> 32); break;
-    case 8: v = (uint32_t)h; break;
-    case 9: v = (uint32_t)(wn.found ? J.it[wn.ii].it : J.final_iteration); break;
-    default: v = (lane & 1) ? (uint32_t)(dbits >> 32) : (uint32_t)dbits; break;
-  }
+  // a chain of selects rather than a switch on the lane, which would run its
+  // cases one after another
+  const uint32_t f_tam = (uint32_t)(wn.found ? J.it[wn.ii].tam : J.final_tam);
+  const uint32_t f_it = (uint32_t)(wn.found ? J.it[wn.ii].it : J.final_iteration);
+  uint32_t v = (lane & 1) ? (uint32_t)(dbits >> 32) : (uint32_t)dbits;
+  v = lane == 9 ? f_it : v;
+  v = lane == 8 ? (uint32_t)h : v;
+  v = lane == 7 ? (uint32_t)(tested >> 32) : v;
+  v = lane == 6 ? (uint32_t)tested : v;
+  v = lane == 5 ? f_tam : v;
+  v = lane == 4 ? (uint32_t)is_equal : v;
+  v = lane == 3 ? (uint32_t)degenerate : v;
+  v = lane == 2 ? (uint32_t)J.original_weight : v;
+  v = lane == 1 ? (uint32_t)w : v;
+  v = lane == 0 ? (uint32_t)wn.found : v;
   static_assert(sizeof(GrandDecoderResult) == 72, "result layout");
   if (lane < 18) reinterpret_cast<uint32_t *>(b.results + shot)[lane] = v;
   if (lane == 0) {
