@@ -552,7 +552,7 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
       prefetch_next_record(b, __shfl_sync(kFull, (int)nxt, 0));
       __syncwarp();
       if (cd.input_kind == kInErrors) {
-        for (int q = 0; q < cd.mw; ++q) {
+        for (int q = 0; q < cd.mw && original_weight != 0; ++q) {
           uint32_t word = A.eb[q];
           while (word) {
             const int c = q * 32 + __ffs(word) - 1;
@@ -567,8 +567,9 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
       original_weight = pack_ballots(rec, cd.m, A.eb);
       prefetch_next_record(b, __shfl_sync(kFull, (int)nxt, 0));
       __syncwarp();
-      // s = XOR of the columns of the supplied error (grand_decoder.cu:476-486)
-      for (int q = 0; q < cd.mw; ++q) {
+      // s = XOR of the columns of the supplied error (grand_decoder.cu:476-486);
+      // an error-free record (most shots at low error rates) skips the walk
+      for (int q = 0; q < cd.mw && original_weight != 0; ++q) {
         uint32_t word = A.eb[q];
         while (word) {
           const int c = q * 32 + __ffs(word) - 1;
@@ -586,19 +587,16 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
       s_lane = lane < cd.nw ? A.sw[lane] : 0u;
     }
     A.sw[lane] = (lane < cd.nw) ? s_lane : 0u;
-    int ws = __popc(s_lane);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) ws += __shfl_xor_sync(kFull, ws, o);
+    const bool empty = !__any_sync(kFull, s_lane != 0u);  // lanes >= nw hold 0
     __syncwarp();
 
-    if (ws == 0) {  // grand_decoder.cu:1223-1241: nothing to search
-      if (lane == 0) {
-        GrandDecoderResult r = {};
-        r.original_weight = original_weight;
-        r.hibrido = -2;
-        b.results[shot] = r;
-        if (b.ml_cost) b.ml_cost[shot] = 0.0f;
-      }
+    if (empty) {  // grand_decoder.cu:1223-1241: nothing to search
+      // the 72-byte result as 18 words, one per lane: original_weight (word 2)
+      // and hibrido = -2 (word 8), everything else 0
+      if (lane < 18)
+        reinterpret_cast<uint32_t *>(b.results + shot)[lane] =
+            lane == 2 ? (uint32_t)original_weight : (lane == 8 ? (uint32_t)-2 : 0u);
+      if (lane == 0 && b.ml_cost) b.ml_cost[shot] = 0.0f;
       if (b.dec_err)
         for (int c = lane; c < cd.m; c += 32) b.dec_err[(size_t)shot * cd.m + c] = 0;
       if (b.dec_log && cd.family == kDem)
