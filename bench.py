@@ -492,7 +492,7 @@ def _time_device(torch, eng, n, d_rec, d_res, sp, flush, steps, warmup, d_sc=0, 
 
 
 def bench_batching(torch, lib, dev, sp, flush):
-    """configs[3]: 100k shots mixing BB[[72]], [[108]] (W=3), [[144]], [[288]] (W=4) at
+    """Mixed-code batch: 100k shots mixing BB[[72]], [[108]] (W=3), [[144]], [[288]] (W=4) at
     p = 0.003, shuffled, in one persistent launch (tuned, graph-replayed) vs the plain
     paths: one C ABI call per code, and one call (one launch pair) per shot."""
     from library_s_grand_gb300 import autotune, capi, synth
@@ -564,7 +564,7 @@ def bench_batching(torch, lib, dev, sp, flush):
 
 
 def bench_ml(torch, lib, dev, sp, flush):
-    """configs[2]: grand_decode_ML_cln on the 120 x 720 random DEM, 65536 shots, W=3."""
+    """ML DEM batch: grand_decode_ML_cln on the 120 x 720 random DEM, 65536 shots, W=3."""
     from library_s_grand_gb300 import capi, synth
     from library_s_grand_gb300.engine import Engine
     dem = synth.random_dem(0)
@@ -643,7 +643,7 @@ def bench_sampling(torch, lib, dev, sp):
 
 
 def bench_serving(lib):
-    """configs[4]: Poisson arrivals of 1-256-shot requests over four BB codes (W=3,
+    """Serving: Poisson arrivals of 1-256-shot requests over four BB codes (W=3,
     syndrome records) and the 120 x 720 DEM in ML mode, offered load swept to
     saturation through the continuous-batching server."""
     from library_s_grand_gb300 import capi, synth
