@@ -606,11 +606,21 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
       continue;
     }
 
-    // sketch of the syndrome: XOR of the row hashes of its set rows
-    uint32_t hs = 0u;
-    for (uint32_t word = s_lane; word; word &= word - 1u) hs ^= row_hash(lane * 32 + __ffs(word) - 1);
+    // Sketch of the syndrome (XOR of the row hashes of its set rows), read by
+    // the sketch scans only: a one-position iteration compares its column with
+    // the syndrome itself, so most shots never form it.
+    bool have_hs = false;
+    auto syndrome_sketch = [&]() {
+      if (have_hs) return;
+      uint32_t hs = 0u;
+      for (uint32_t word = s_lane; word; word &= word - 1u)
+        hs ^= row_hash(lane * 32 + __ffs(word) - 1);
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) hs ^= __shfl_xor_sync(kFull, hs, o);
+      for (int o = 16; o > 0; o >>= 1) hs ^= __shfl_xor_sync(kFull, hs, o);
+      if (lane == 0) J.hs = hs;
+      __syncwarp();
+      have_hs = true;
+    };
 
     // ---- flagged-check counts and threshold masks ---------------------------
     const int L = cd.max_soma < kMaxIters ? cd.max_soma : kMaxIters;
@@ -683,7 +693,6 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
       J.original_weight = original_weight;
       J.best = kNone;
       J.tiles_done = 0;
-      J.hs = hs;
       J.t_start = t_start;
       J.t_counts = global_ns();
     }
@@ -716,7 +725,10 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
         break;
       }
       if (!ml && I.tam == 1) single_search(cd, J, A, ii, wn);
-      else light_search<MLK>(b, cd, J, A, ii, wn);
+      else {
+        syndrome_sketch();
+        light_search<MLK>(b, cd, J, A, ii, wn);
+      }
       if (wn.found) break;
     }
     if (heavy_from < 0) {
@@ -727,6 +739,7 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
     }
 
     // ---- heavy: publish a Job ------------------------------------------------
+    syndrome_sketch();
     unsigned long long words = 0;
     for (int ii = heavy_from; ii < J.n_it; ++ii) {
       const unsigned long long tm = (unsigned long long)J.it[ii].tam;
