@@ -84,7 +84,7 @@ __device__ int plan_next(const DevCode &cd, int tam0, int tam1, int tam2, int L,
       S.cum = nullptr;
       S.K = S.runs ? kRunKK : tile_k;
       // run-tile counts are built by the warp when a Job is published; colex
-      // blocks (w <= 2) have at most tam - 1 prefixes, so 32-bit division does
+      // blocks (w <= 2) have at most tam - 1 prefixes, so a 32-bit division suffices
       S.ntiles = S.runs ? 0ull
                         : (unsigned long long)(((unsigned)S.nprefix + 32u * (unsigned)S.K - 1u) /
                                                (32u * (unsigned)S.K));
