@@ -1,9 +1,12 @@
-"""The search kernels' warp-free index math, compiled for the host from the
-CUDA header itself (csrc/grand_device.cuh) and checked against plain
-combinatorics and a brute-force search (tests/host_device_math.cpp): binomials,
-colex unranking in closed form and by table, colex successors, lexicographic
-ranks, the FP32 cost key, and whole run tiles lane by lane, first-hit and ML.
-Runs without a GPU."""
+"""The search kernels' device code, compiled for the host from the CUDA header
+itself (csrc/grand_device.cuh) and checked against plain combinatorics and a
+brute-force search, without a GPU:
+  tests/host_device_math.cpp  warp-free math: binomials, colex unranking in
+      closed form and by table, colex successors, lexicographic ranks, the FP32
+      cost key, and whole run tiles lane by lane, first-hit and ML;
+  tests/host_warp_math.cpp    warp-level code on an emulated warp (32 host
+      threads whose collectives meet at a barrier): the warp minima, the result
+      writer's warp-parallel unranking, and whole masked colex tiles."""
 import os
 import shutil
 import subprocess
@@ -21,17 +24,25 @@ def _cuda_include():
     return None
 
 
-def test_device_index_math_on_host(tmp_path):
+def _build_and_run(tmp_path, source, std, extra=()):
     cxx = shutil.which("g++")
     inc = _cuda_include()
     if cxx is None or inc is None:
         pytest.skip("needs g++ and the CUDA headers")
-    exe = str(tmp_path / "device_math")
-    subprocess.run([cxx, "-std=c++17", "-O2",
+    exe = str(tmp_path / os.path.splitext(source)[0])
+    subprocess.run([cxx, f"-std={std}", "-O2", *extra,
                     "-I", os.path.join(ROOT, "library_s_grand_gb300", "csrc"),
                     "-I", os.path.join(ROOT, "include"), "-I", inc,
-                    os.path.join(HERE, "host_device_math.cpp"), "-o", exe],
+                    os.path.join(HERE, source), "-o", exe],
                    check=True, capture_output=True, text=True)
     out = subprocess.run([exe], capture_output=True, text=True, timeout=300)
     assert out.returncode == 0, out.stderr
     assert out.stdout.startswith("ok"), out.stdout
+
+
+def test_device_index_math_on_host(tmp_path):
+    _build_and_run(tmp_path, "host_device_math.cpp", "c++17")
+
+
+def test_warp_level_device_code_on_an_emulated_warp(tmp_path):
+    _build_and_run(tmp_path, "host_warp_math.cpp", "c++20", ["-pthread"])
