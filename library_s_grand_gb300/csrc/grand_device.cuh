@@ -28,9 +28,13 @@ constexpr unsigned long long kNone = ~0ull;
 
 // Nanoseconds of the GPU's global timer (the per-shot timing fields).
 __device__ __forceinline__ unsigned long long global_ns() {
+#ifdef GRAND_HOST_EMULATION  // the host build of the kernels used by the CPU tests
+  return 0ull;
+#else
   unsigned long long t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
+#endif
 }
 
 __device__ __forceinline__ unsigned long long ncr(const unsigned long long *t, int n, int k) {
@@ -527,6 +531,9 @@ __device__ __forceinline__ bool atomic_min_key(unsigned long long *slot, uint32_
   for (int guard = 0; guard < (1 << 20); ++guard) {
     if ((unsigned long long)o > cur0 || ((unsigned long long)o == cur0 && r >= cur1)) return true;
     unsigned long long got0, got1;
+#ifdef GRAND_HOST_EMULATION  // the host build supplies the 128-bit CAS
+    grand_host_cas128(slot, cur0, cur1, (unsigned long long)o, r, &got0, &got1);
+#else
     asm volatile(
         "{\n\t.reg .b128 d, c, n;\n\t"
         "mov.b128 c, {%2, %3};\n\t"
@@ -536,6 +543,7 @@ __device__ __forceinline__ bool atomic_min_key(unsigned long long *slot, uint32_
         : "=l"(got0), "=l"(got1)
         : "l"(cur0), "l"(cur1), "l"((unsigned long long)o), "l"(r), "l"(slot)
         : "memory");
+#endif
     if (got0 == cur0 && got1 == cur1) return true;
     cur0 = got0;
     cur1 = got1;

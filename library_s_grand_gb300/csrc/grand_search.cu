@@ -177,7 +177,8 @@ __global__ void __launch_bounds__(kSearchThreads, 3) search_kernel(DevBatch b) {
         skip_known = false;
       }
       if (!skip_known || s_ml) {
-        skip = tile_skip(J, J.seg[cs], J.it[s_iter], s_ml);
+        // one decision for the warp: other warps lower the bound while lanes read it
+        skip = __any_sync(kFull, tile_skip(J, J.seg[cs], J.it[s_iter], s_ml));
         skip_known = true;
       }
       bool published = false;
@@ -259,6 +260,7 @@ __global__ void __launch_bounds__(kSearchThreads, 3) search_kernel(DevBatch b) {
 // ---------------------------------------------------------------------------
 // Host-callable launcher.
 // ---------------------------------------------------------------------------
+#ifndef GRAND_HOST_EMULATION  // launchers: device builds only
 cudaError_t launch_search(const DevBatch &b, int grid, cudaStream_t s) {
   if (b.has_ml) search_kernel<true><<<grid, kSearchThreads, 0, s>>>(b);
   else search_kernel<false><<<grid, kSearchThreads, 0, s>>>(b);
@@ -273,5 +275,7 @@ cudaError_t occupancy(int *triage_blocks_per_sm, int *search_blocks_per_sm) {
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(search_blocks_per_sm, search_kernel<true>,
                                                        kSearchThreads, 0);
 }
+
+#endif
 
 }  // namespace grand

@@ -220,9 +220,11 @@ __device__ __forceinline__ void prefetch_next_record(const DevBatch &b, int slot
   const char *p = reinterpret_cast<const char *>(
       b.in + (b.in_off ? b.in_off[shot] : (long long)shot * len));
   const int nbytes = len * 4;
+#ifndef GRAND_HOST_EMULATION  // a hint only: the host build of the kernels skips it
   for (int o = lane * 128; o < nbytes; o += 32 * 128)
     asm volatile("prefetch.global.L2 [%0];" ::"l"(p + o));
   if (lane == 0 && nbytes > 0) asm volatile("prefetch.global.L2 [%0];" ::"l"(p + nbytes - 1));
+#endif
 }
 
 // ---------------------------------------------------------------------------
@@ -710,6 +712,7 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
     int heavy_from = -1;
     for (;;) {
       int more = 0;
+      __syncwarp();  // every lane is done reading the Job before lane 0 extends it
       if (lane == 0) more = plan_next(cd, tam_raw[0], tam_raw[1], tam_raw[2], L, b.tile_k, J, P);
       more = __shfl_sync(kFull, more, 0);
       __syncwarp();
@@ -718,6 +721,7 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
       const IterInfo &I = J.it[ii];
       if (I.total > budget || I.tam > kLightTam || I.tam * cd.nwp > kLightWords) {
         heavy_from = ii;
+        __syncwarp();  // every lane has read n_it before lane 0 plans the rest
         if (lane == 0)
           while (plan_next(cd, tam_raw[0], tam_raw[1], tam_raw[2], L, b.tile_k, J, P)) {
           }
@@ -877,6 +881,7 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
 // ---------------------------------------------------------------------------
 // Host-callable launcher.
 // ---------------------------------------------------------------------------
+#ifndef GRAND_HOST_EMULATION  // launchers: device builds only
 cudaError_t launch_triage(const DevBatch &b, int grid, cudaStream_t s) {
   if (b.has_ml) triage_kernel<true><<<grid, kTriageWarps * 32, 0, s>>>(b);
   else triage_kernel<false><<<grid, kTriageWarps * 32, 0, s>>>(b);
@@ -889,5 +894,7 @@ cudaError_t triage_occupancy(int *blocks_per_sm) {
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, triage_kernel<true>,
                                                        kTriageWarps * 32, 0);
 }
+
+#endif
 
 }  // namespace grand

@@ -1,0 +1,378 @@
+// Host build of the two decoding kernels (csrc/grand_triage.cu, grand_search.cu)
+// on emulated warps, for the CPU parity tests (tests/test_host_kernels.py).
+//
+// Each kernel runs as one thread block: one host thread per lane, the lanes of
+// a warp meeting at a barrier in every warp collective (ballot, shuffles,
+// reductions, votes, __syncwarp), the block's __shared__ arrays as static
+// storage, device atomics as host atomics.  The kernels' code keeps its lanes
+// converged at every collective, so it runs here as on the GPU, the order of
+// the warps' work aside (which never changes a result: every search result is
+// an exact minimum).  Code tables are built as the library builds them.
+//
+// Usage: host_kernels DIR   reads DIR/params.txt, DIR/H.bin, DIR/Hother.bin,
+// DIR/rec.bin (int32), writes DIR/res.bin (72-byte results) and DIR/dec.bin
+// (decoded errors, one byte per column and shot).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <functional>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+// ---- thread and warp emulation ------------------------------------------------
+struct Idx3 {
+  unsigned x, y, z;
+};
+static thread_local Idx3 threadIdx;
+static Idx3 blockIdx = {0, 0, 0}, blockDim = {0, 1, 1}, gridDim = {1, 1, 1};
+
+// a warp's meeting point: the last lane to arrive opens the next generation;
+// the others spin briefly, then yield (lanes far outnumber host cores)
+struct LaneBarrier {
+  std::atomic<int> count{0}, gen{0};
+  void arrive_and_wait() {
+    const int g = gen.load(std::memory_order_acquire);
+    if (count.fetch_add(1, std::memory_order_acq_rel) == 31) {
+      count.store(0, std::memory_order_relaxed);
+      gen.fetch_add(1, std::memory_order_release);
+      return;
+    }
+    for (int spin = 0; gen.load(std::memory_order_acquire) == g; ++spin)
+      if (spin > 64) std::this_thread::yield();
+  }
+};
+struct WarpState {
+  LaneBarrier bar;
+  unsigned long long v[32];
+};
+static thread_local WarpState *tl_warp = nullptr;
+
+template <class F>
+static auto collective(unsigned long long mine, F f) {
+  const unsigned lane = threadIdx.x & 31;
+  tl_warp->v[lane] = mine;
+  tl_warp->bar.arrive_and_wait();
+  auto r = f(tl_warp->v, lane);
+  tl_warp->bar.arrive_and_wait();
+  return r;
+}
+static inline void __syncwarp(unsigned = 0xffffffffu) { tl_warp->bar.arrive_and_wait(); }
+static inline unsigned __ballot_sync(unsigned, int p) {
+  return collective((unsigned long long)(p != 0), [](const unsigned long long *v, unsigned) {
+    unsigned m = 0;
+    for (int i = 0; i < 32; ++i) m |= (unsigned)(v[i] & 1ull) << i;
+    return m;
+  });
+}
+static inline int __any_sync(unsigned m, int p) { return __ballot_sync(m, p) != 0u; }
+static inline int __all_sync(unsigned m, int p) { return __ballot_sync(m, p) == 0xffffffffu; }
+template <class T>
+static inline T __shfl_sync(unsigned, T x, int src) {
+  unsigned long long u = 0;
+  memcpy(&u, &x, sizeof(T));
+  return collective(u, [src](const unsigned long long *v, unsigned) {
+    T r;
+    memcpy(&r, &v[src & 31], sizeof(T));
+    return r;
+  });
+}
+template <class T>
+static inline T __shfl_xor_sync(unsigned, T x, int m) {
+  unsigned long long u = 0;
+  memcpy(&u, &x, sizeof(T));
+  return collective(u, [m](const unsigned long long *v, unsigned lane) {
+    T r;
+    memcpy(&r, &v[(lane ^ (unsigned)m) & 31], sizeof(T));
+    return r;
+  });
+}
+template <class T>
+static inline T __shfl_up_sync(unsigned, T x, unsigned d) {
+  unsigned long long u = 0;
+  memcpy(&u, &x, sizeof(T));
+  return collective(u, [d](const unsigned long long *v, unsigned lane) {
+    T r;
+    memcpy(&r, &v[lane >= d ? lane - d : lane], sizeof(T));
+    return r;
+  });
+}
+static inline unsigned __reduce_min_sync(unsigned, unsigned x) {
+  return collective(x, [](const unsigned long long *v, unsigned) {
+    unsigned r = 0xffffffffu;
+    for (int i = 0; i < 32; ++i) r = std::min(r, (unsigned)v[i]);
+    return r;
+  });
+}
+static inline unsigned __reduce_max_sync(unsigned, unsigned x) {
+  return collective(x, [](const unsigned long long *v, unsigned) {
+    unsigned r = 0u;
+    for (int i = 0; i < 32; ++i) r = std::max(r, (unsigned)v[i]);
+    return r;
+  });
+}
+static inline int __clz(unsigned x) { return x ? __builtin_clz(x) : 32; }
+static inline int __ffs(unsigned x) { return __builtin_ffs((int)x); }
+static inline int __popc(unsigned x) { return __builtin_popcount(x); }
+static inline float __fadd_rn(float a, float b) { return a + b; }
+static inline unsigned __float_as_uint(float f) {
+  unsigned u;
+  memcpy(&u, &f, 4);
+  return u;
+}
+static inline float __uint_as_float(unsigned u) {
+  float f;
+  memcpy(&f, &u, 4);
+  return f;
+}
+static inline long long __double_as_longlong(double d) {
+  long long u;
+  memcpy(&u, &d, 8);
+  return u;
+}
+static inline unsigned __vimin3_u32(unsigned a, unsigned b, unsigned c) {
+  return std::min(a, std::min(b, c));
+}
+template <class T>
+static inline T __ldg(const T *p) {
+  T r;
+  memcpy(&r, p, sizeof(T));
+  return r;
+}
+template <class T>
+static inline T __ldcg(const T *p) {
+  T r;
+  memcpy(&r, p, sizeof(T));
+  return r;
+}
+static inline unsigned min(unsigned a, unsigned b) { return a < b ? a : b; }
+static inline int min(int a, int b) { return a < b ? a : b; }
+static inline void __threadfence() { __atomic_thread_fence(__ATOMIC_SEQ_CST); }
+static inline unsigned long long atomicAdd(unsigned long long *a, unsigned long long v) {
+  return __atomic_fetch_add(a, v, __ATOMIC_SEQ_CST);
+}
+static inline unsigned atomicAdd(unsigned *a, unsigned v) {
+  return __atomic_fetch_add(a, v, __ATOMIC_SEQ_CST);
+}
+static inline unsigned atomicOr(unsigned *a, unsigned v) {
+  return __atomic_fetch_or(a, v, __ATOMIC_SEQ_CST);
+}
+static inline unsigned long long atomicMin(unsigned long long *a, unsigned long long v) {
+  unsigned long long cur = __atomic_load_n(a, __ATOMIC_SEQ_CST);
+  while (v < cur &&
+         !__atomic_compare_exchange_n(a, &cur, v, false, __ATOMIC_SEQ_CST, __ATOMIC_SEQ_CST)) {
+  }
+  return cur;
+}
+static inline unsigned atomicCAS(unsigned *a, unsigned cmp, unsigned v) {
+  __atomic_compare_exchange_n(a, &cmp, v, false, __ATOMIC_SEQ_CST, __ATOMIC_SEQ_CST);
+  return cmp;
+}
+static std::mutex g_cas_mu;
+static inline void grand_host_cas128(unsigned long long *slot, unsigned long long c0,
+                                     unsigned long long c1, unsigned long long n0,
+                                     unsigned long long n1, unsigned long long *g0,
+                                     unsigned long long *g1) {
+  std::lock_guard<std::mutex> lk(g_cas_mu);
+  *g0 = slot[0];
+  *g1 = slot[1];
+  if (*g0 == c0 && *g1 == c1) {
+    slot[0] = n0;
+    slot[1] = n1;
+  }
+}
+
+// a block's __shared__ arrays: static storage shared by the block's host threads
+#undef __shared__
+#define __shared__ static
+#ifndef __launch_bounds__
+#define __launch_bounds__(...)
+#endif
+
+#define GRAND_HOST_EMULATION 1
+#include "grand_triage.cu"
+#include "grand_search.cu"
+
+using namespace grand;
+
+// run body on blockDim.x host threads, one emulated warp per 32 lanes
+static void run_block(int threads, const std::function<void()> &body) {
+  blockDim.x = (unsigned)threads;
+  std::vector<WarpState> warps(threads / 32);
+  std::vector<std::thread> th;
+  for (int t = 0; t < threads; ++t)
+    th.emplace_back([&, t] {
+      threadIdx.x = (unsigned)t;
+      tl_warp = &warps[t / 32];
+      body();
+    });
+  for (auto &x : th) x.join();
+}
+
+static std::vector<int> read_ints(const std::string &path, size_t n) {
+  std::vector<int> v(n);
+  FILE *f = fopen(path.c_str(), "rb");
+  if (!f || fread(v.data(), 4, n, f) != n) {
+    fprintf(stderr, "cannot read %s\n", path.c_str());
+    exit(2);
+  }
+  fclose(f);
+  return v;
+}
+
+static unsigned long long C(int n, int k) {
+  if (k < 0 || n < k) return 0;
+  unsigned long long r = 1;
+  for (int i = 1; i <= k; ++i) r = r * (unsigned long long)(n - k + i) / (unsigned long long)i;
+  return r;
+}
+
+int main(int argc, char **argv) {
+  if (argc != 2) return 2;
+  const std::string dir = argv[1];
+  FILE *pf = fopen((dir + "/params.txt").c_str(), "r");
+  if (!pf) return 2;
+  int variant, input_kind, n, m, N, W, mode, thr, cap, num_phases, n_masks, light, tile_k;
+  if (fscanf(pf, "%d %d %d %d %d %d %d %d %d %d %d %d %d", &variant, &input_kind, &n, &m, &N, &W,
+             &mode, &thr, &cap, &num_phases, &n_masks, &light, &tile_k) != 13)
+    return 2;
+  DevCode d;
+  memset(&d, 0, sizeof(d));
+  for (int q = 0; q < n_masks; ++q)
+    if (fscanf(pf, "%d %d %d %d", &d.mask_tam_upper[q], &d.mask_order[q][0], &d.mask_order[q][1],
+               &d.mask_order[q][2]) != 4)
+      return 2;
+  fclose(pf);
+  const std::vector<int> H = read_ints(dir + "/H.bin", (size_t)n * m);
+  const std::vector<int> Ho = read_ints(dir + "/Hother.bin", (size_t)n * m);
+  const int rec_len = input_kind == kInErrors ? m : n;
+  const std::vector<int> rec = read_ints(dir + "/rec.bin", (size_t)N * rec_len);
+
+  // code tables, built as the library builds them for a CSS code
+  const int nw = (n + 31) / 32;
+  const int nwp = nw <= 2 ? nw : (nw <= 4 ? 4 : (nw <= 8 ? 8 : (nw + 3) & ~3));
+  const int mw = (m + 31) / 32;
+  std::vector<uint32_t> cols((size_t)m * nwp, 0u), hcol(m, 0u);
+  std::vector<int> colw(m, 0);
+  for (int r = 0; r < n; ++r)
+    for (int c = 0; c < m; ++c)
+      if (H[(size_t)r * m + c] != 0) {
+        ++colw[c];
+        cols[(size_t)c * nwp + (r >> 5)] |= 1u << (r & 31);
+        hcol[c] ^= row_hash(r);
+      }
+  int max_soma = 0, regular = 1;
+  for (int c = 0; c < m; ++c) max_soma = std::max(max_soma, colw[c]);
+  for (int c = 1; c < m; ++c)
+    if (colw[c] != colw[0]) regular = 0;
+  std::vector<uint32_t> rows((size_t)n * mw, 0u);
+  for (int r = 0; r < n; ++r)
+    for (int c = 0; c < m; ++c)
+      if (Ho[(size_t)r * m + c] & 1) rows[(size_t)r * mw + (c >> 5)] |= 1u << (c & 31);
+  std::vector<int> pivrow(m, -1);
+  int rank = 0;
+  for (int c = 0; c < m && rank < n; ++c) {  // reduced row echelon form over GF(2)
+    const int q = c >> 5;
+    const uint32_t bit = 1u << (c & 31);
+    int p = -1;
+    for (int i = rank; i < n; ++i)
+      if (rows[(size_t)i * mw + q] & bit) {
+        p = i;
+        break;
+      }
+    if (p < 0) continue;
+    for (int j = 0; j < mw; ++j) std::swap(rows[(size_t)rank * mw + j], rows[(size_t)p * mw + j]);
+    for (int i = 0; i < n; ++i)
+      if (i != rank && (rows[(size_t)i * mw + q] & bit))
+        for (int j = 0; j < mw; ++j) rows[(size_t)i * mw + j] ^= rows[(size_t)rank * mw + j];
+    pivrow[c] = rank++;
+  }
+
+  d.R = n;
+  d.m = m;
+  d.nw = nw;
+  d.nwp = nwp;
+  d.mw = mw;
+  d.max_soma = max_soma;
+  d.regular = regular;
+  d.family = kCss;
+  d.variant = variant;
+  d.input_kind = input_kind;
+  d.W = W;
+  d.Wc = std::min(W, (int)kMaxW);
+  d.mode = mode;
+  d.thr = thr;
+  d.cap = cap;
+  d.num_phases = num_phases;
+  d.n_masks = n_masks;
+  d.rank = rank;
+  d.rec_len = rec_len;
+  d.cols = cols.data();
+  d.colw = colw.data();
+  d.rref = rows.data();
+  d.pivrow = pivrow.data();
+  d.hcol = hcol.data();
+
+  std::vector<unsigned long long> ncr((size_t)(kMaxTam + 1) * (kMaxW + 1));
+  for (int a = 0; a <= kMaxTam; ++a)
+    for (int k = 0; k <= kMaxW; ++k) ncr[(size_t)a * (kMaxW + 1) + k] = C(a, k);
+  std::vector<GrandDecoderResult> res(N);
+  std::vector<unsigned char> dec((size_t)N * m, 0);
+  const int max_jobs = std::max(N, 1);
+  std::vector<Job> jobs(max_jobs);
+  alignas(16) static unsigned long long small[32];
+  memset(small, 0, sizeof(small));
+  const unsigned long long scratch_words = 8ull << 20;
+  std::vector<uint32_t> scratch(scratch_words);
+  std::vector<int> deferred(N, 0);
+
+  DevBatch b;
+  memset(&b, 0, sizeof(b));
+  b.num_shots = N;
+  b.num_codes = 1;
+  b.codes = &d;
+  b.in = rec.data();
+  b.results = res.data();
+  b.dec_err = dec.data();
+  b.ncr = ncr.data();
+  b.jobs = jobs.data();
+  b.max_jobs = max_jobs;
+  b.counters = small;
+  b.status = reinterpret_cast<unsigned *>(reinterpret_cast<char *>(small) + 128);
+  b.scratch = scratch.data();
+  b.scratch_words = scratch_words;
+  b.deferred = deferred.data();
+  b.light_max_log2 = light;
+  b.tile_k = tile_k;
+  b.has_ml = variant == kMl;
+
+  run_block(kTriageWarps * 32, [&] {
+    if (b.has_ml) triage_kernel<true>(b);
+    else triage_kernel<false>(b);
+  });
+  run_block(kSearchThreads, [&] {
+    if (b.has_ml) search_kernel<true>(b);
+    else search_kernel<false>(b);
+  });
+  const unsigned status = *b.status;
+  for (int i = 0; i < N; ++i)
+    if (deferred[i]) {
+      fprintf(stderr, "shot %d deferred (status %u)\n", i, status);
+      return 3;
+    }
+  FILE *f = fopen((dir + "/res.bin").c_str(), "wb");
+  fwrite(res.data(), sizeof(GrandDecoderResult), N, f);
+  fclose(f);
+  f = fopen((dir + "/dec.bin").c_str(), "wb");
+  fwrite(dec.data(), 1, dec.size(), f);
+  fclose(f);
+  printf("ok %d shots, %llu jobs, status %u\n", N, small[0] >> 40, status);
+  return 0;
+}

@@ -9,7 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
-#include <barrier>
+#include <atomic>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -26,8 +26,23 @@ struct LaneIndex {
 static thread_local LaneIndex threadIdx;
 
 // ---- the emulated warp ------------------------------------------------------
+// the warp's meeting point: the last lane to arrive opens the next generation;
+// the others spin briefly, then yield (lanes outnumber host cores)
+struct LaneBarrier {
+  std::atomic<int> count{0}, gen{0};
+  void arrive_and_wait() {
+    const int g = gen.load(std::memory_order_acquire);
+    if (count.fetch_add(1, std::memory_order_acq_rel) == 31) {
+      count.store(0, std::memory_order_relaxed);
+      gen.fetch_add(1, std::memory_order_release);
+      return;
+    }
+    for (int spin = 0; gen.load(std::memory_order_acquire) == g; ++spin)
+      if (spin > 64) std::this_thread::yield();
+  }
+};
 struct WarpState {
-  std::barrier<> bar{32};
+  LaneBarrier bar;
   unsigned long long v[32];
 };
 static WarpState *g_warp = nullptr;

@@ -1,0 +1,102 @@
+"""CPU parity of the decoding kernels themselves: grand_triage.cu and
+grand_search.cu compiled for the host (tests/host_kernels.cpp: one thread block
+per kernel, one host thread per lane, warp collectives at a barrier) and run on
+CSS shots whose results must equal the oracle's in every deterministic field
+and decoded pattern.  A small light budget sends most iterations through the
+search kernel (run tiles, colex tiles, the Job finisher) as well as the triage
+warp's paths (empty shots, one-position iterations, bit-mask enumeration).
+Runs without a GPU."""
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle as O
+from library_s_grand_gb300 import capi, synth
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+
+
+def _cuda_include():
+    for base in (os.environ.get("CUDA_HOME"), os.environ.get("CUDA_PATH"), "/usr/local/cuda"):
+        if base and os.path.exists(os.path.join(base, "include", "cuda_runtime.h")):
+            return os.path.join(base, "include")
+    return None
+
+
+@pytest.fixture(scope="module")
+def emulator(tmp_path_factory):
+    cxx, inc = shutil.which("g++"), _cuda_include()
+    if cxx is None or inc is None:
+        pytest.skip("needs g++ and the CUDA headers")
+    exe = str(tmp_path_factory.mktemp("hk") / "host_kernels")
+    subprocess.run([cxx, "-std=c++20", "-O2", "-pthread",
+                    "-I", os.path.join(ROOT, "library_s_grand_gb300", "csrc"),
+                    "-I", os.path.join(ROOT, "include"), "-I", inc,
+                    os.path.join(HERE, "host_kernels.cpp"), "-o", exe],
+                   check=True, capture_output=True, text=True)
+    return exe
+
+
+def _num_phases(W):  # upstream's phase count per max weight
+    return {6: 2, 7: 3}.get(W, 1 if 0 < W < 6 else 0)
+
+
+def _run(exe, d, H, Ho, records, errors_input, variant, cfg, masks, light, tile_k=4):
+    W, _, _, cap, thr, mode = cfg
+    n, m = H.shape
+    N = records.shape[0]
+    with open(os.path.join(d, "params.txt"), "w") as f:
+        f.write(f"{variant} {1 if errors_input else 0} {n} {m} {N} {W} {mode} {thr} {cap} "
+                f"{_num_phases(W) if variant == 1 else 0} {len(masks)} {light} {tile_k}\n")
+        for row in masks:
+            f.write(" ".join(str(int(v)) for v in row[:4]) + "\n")
+    np.ascontiguousarray(H, dtype=np.int32).tofile(os.path.join(d, "H.bin"))
+    np.ascontiguousarray(Ho, dtype=np.int32).tofile(os.path.join(d, "Hother.bin"))
+    np.ascontiguousarray(records, dtype=np.int32).tofile(os.path.join(d, "rec.bin"))
+    out = subprocess.run([exe, d], capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr + out.stdout
+    res = np.fromfile(os.path.join(d, "res.bin"), dtype=capi.RESULT_DTYPE)
+    dec = np.fromfile(os.path.join(d, "dec.bin"), dtype=np.uint8).reshape(N, m)
+    return res, dec, out.stdout
+
+
+def _compare(res, dec, pres, pdec):
+    bad = O.fields_equal(res, pres)
+    assert len(bad) == 0, f"shots {bad[:5]}\nemulated {res[bad[:3]]}\noracle {pres[bad[:3]]}"
+    diff = np.nonzero((dec != pdec).any(axis=1))[0]
+    assert len(diff) == 0, f"decoded patterns differ on shots {diff[:5]}"
+
+
+@pytest.mark.parametrize("W,mode,thr,cap,light", [(4, -1, 10, 64, 3), (3, 0, 10, 64, 5),
+                                                  (4, 1, 8, 24, 12), (5, -1, 10, 64, 4)])
+def test_uniform_errors(emulator, port, tmp_path, W, mode, thr, cap, light):
+    code = synth.BB_CODES[72]()
+    errors = np.concatenate([synth.css_shots(code.hz, 60, p, seed=900 + i)[0]
+                             for i, p in enumerate((0.01, 0.03, 0.06))])
+    cfg = (W, 256, 0, cap, thr, mode)
+    res, dec, log = _run(emulator, str(tmp_path), code.hz, code.hx, errors, True, 0, cfg, [], light)
+    prc, pres, pdec = port.css(O.UNIFORM, code.hx, code.hz, errors, None, O.Config(*cfg), "x")
+    assert prc == 0
+    _compare(res, dec, pres, pdec)
+    assert int(log.split()[3]) > 0 or light >= 12, log  # the search kernel had Jobs
+
+
+def test_prob_syndromes(emulator, port, tmp_path):
+    code = synth.BB_CODES[108]()
+    errors = np.concatenate([synth.css_shots(code.hz, 60, p, seed=950 + i)[0]
+                             for i, p in enumerate((0.01, 0.03))])
+    syn = (errors.astype(np.int64) @ code.hz.T.astype(np.int64) % 2).astype(np.int32)
+    masks = [(9, 0, 1, 2, 0.5, 0.3, 0.2), (300, 1, 0, 2, 0.6, 0.3, 0.1)]
+    phase = synth.write_phase_file(str(tmp_path / "phase.txt"), masks)
+    cfg = (4, 256, 0, 30, 8, 1)  # mode 1: sets above 30 positions are skipped
+    d = tmp_path / "run"
+    d.mkdir()
+    res, dec, log = _run(emulator, str(d), code.hz, code.hx, syn, False, 1, cfg, masks, 4)
+    prc, pres, pdec = port.css(O.PROB, code.hx, code.hz, None, syn, O.Config(*cfg), "x", phase)
+    assert prc == 0
+    _compare(res, dec, pres, pdec)
+    assert int(log.split()[3]) > 0, log  # the search kernel had Jobs
