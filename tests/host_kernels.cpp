@@ -9,9 +9,12 @@
 // the warps' work aside (which never changes a result: every search result is
 // an exact minimum).  Code tables are built as the library builds them.
 //
-// Usage: host_kernels DIR   reads DIR/params.txt, DIR/H.bin, DIR/Hother.bin,
-// DIR/rec.bin (int32), writes DIR/res.bin (72-byte results) and DIR/dec.bin
-// (decoded errors, one byte per column and shot).
+// Usage: host_kernels DIR   reads DIR/params.txt, DIR/H.bin, DIR/rec.bin (int32
+// records) and, for a CSS code, DIR/Hother.bin (the other check matrix) or, for
+// a DEM, DIR/L.bin (m x n_logicos) and DIR/log.bin (true logical flips), plus
+// DIR/llr.txt for ML; writes DIR/res.bin (72-byte results), DIR/dec.bin (decoded
+// errors, a byte per column and shot) and, for a DEM, DIR/declog.bin (decoded
+// logical flips) and DIR/cost.bin (ML costs, FP32).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -239,9 +242,9 @@ int main(int argc, char **argv) {
   const std::string dir = argv[1];
   FILE *pf = fopen((dir + "/params.txt").c_str(), "r");
   if (!pf) return 2;
-  int variant, input_kind, n, m, N, W, mode, thr, cap, num_phases, n_masks, light, tile_k;
-  if (fscanf(pf, "%d %d %d %d %d %d %d %d %d %d %d %d %d", &variant, &input_kind, &n, &m, &N, &W,
-             &mode, &thr, &cap, &num_phases, &n_masks, &light, &tile_k) != 13)
+  int family, variant, input_kind, n, m, N, W, mode, thr, cap, num_phases, n_masks, light, tile_k, nl;
+  if (fscanf(pf, "%d %d %d %d %d %d %d %d %d %d %d %d %d %d %d", &family, &variant, &input_kind, &n,
+             &m, &N, &W, &mode, &thr, &cap, &num_phases, &n_masks, &light, &tile_k, &nl) != 15)
     return 2;
   DevCode d;
   memset(&d, 0, sizeof(d));
@@ -250,10 +253,22 @@ int main(int argc, char **argv) {
                &d.mask_order[q][2]) != 4)
       return 2;
   fclose(pf);
+  const bool dem = family == kDem;
   const std::vector<int> H = read_ints(dir + "/H.bin", (size_t)n * m);
-  const std::vector<int> Ho = read_ints(dir + "/Hother.bin", (size_t)n * m);
+  const std::vector<int> Ho = dem ? std::vector<int>() : read_ints(dir + "/Hother.bin", (size_t)n * m);
+  const std::vector<int> L = dem ? read_ints(dir + "/L.bin", (size_t)m * nl) : std::vector<int>();
   const int rec_len = input_kind == kInErrors ? m : n;
   const std::vector<int> rec = read_ints(dir + "/rec.bin", (size_t)N * rec_len);
+  const std::vector<int> logicals =
+      dem ? read_ints(dir + "/log.bin", (size_t)N * std::max(nl, 1)) : std::vector<int>();
+  std::vector<float> llr(m, 0.0f);
+  if (variant == kMl) {  // the library's reader: fscanf("%f") per column
+    FILE *lf = fopen((dir + "/llr.txt").c_str(), "r");
+    if (!lf) return 2;
+    for (int i = 0; i < m; ++i)
+      if (fscanf(lf, "%f", &llr[i]) != 1) return 2;
+    fclose(lf);
+  }
 
   // code tables, built as the library builds them for a CSS code
   const int nw = (n + 31) / 32;
@@ -272,13 +287,13 @@ int main(int argc, char **argv) {
   for (int c = 0; c < m; ++c) max_soma = std::max(max_soma, colw[c]);
   for (int c = 1; c < m; ++c)
     if (colw[c] != colw[0]) regular = 0;
-  std::vector<uint32_t> rows((size_t)n * mw, 0u);
-  for (int r = 0; r < n; ++r)
+  std::vector<uint32_t> rows(dem ? 0 : (size_t)n * mw, 0u);
+  for (int r = 0; r < n && !dem; ++r)
     for (int c = 0; c < m; ++c)
       if (Ho[(size_t)r * m + c] & 1) rows[(size_t)r * mw + (c >> 5)] |= 1u << (c & 31);
   std::vector<int> pivrow(m, -1);
   int rank = 0;
-  for (int c = 0; c < m && rank < n; ++c) {  // reduced row echelon form over GF(2)
+  for (int c = 0; c < m && rank < n && !dem; ++c) {  // reduced row echelon form over GF(2)
     const int q = c >> 5;
     const uint32_t bit = 1u << (c & 31);
     int p = -1;
@@ -302,7 +317,16 @@ int main(int argc, char **argv) {
   d.mw = mw;
   d.max_soma = max_soma;
   d.regular = regular;
-  d.family = kCss;
+  const int nlw = (nl + 31) / 32;
+  std::vector<uint32_t> lcols((size_t)m * std::max(nlw, 1), 0u);
+  for (int c = 0; c < m && dem; ++c)
+    for (int j = 0; j < nl; ++j)
+      if (L[(size_t)c * nl + j] != 0) lcols[(size_t)c * nlw + (j >> 5)] |= 1u << (j & 31);
+  d.family = dem ? kDem : kCss;
+  d.n_logicos = nl;
+  d.nlw = nlw;
+  d.lcols = lcols.data();
+  d.llr = llr.data();
   d.variant = variant;
   d.input_kind = input_kind;
   d.W = W;
@@ -324,7 +348,8 @@ int main(int argc, char **argv) {
   for (int a = 0; a <= kMaxTam; ++a)
     for (int k = 0; k <= kMaxW; ++k) ncr[(size_t)a * (kMaxW + 1) + k] = C(a, k);
   std::vector<GrandDecoderResult> res(N);
-  std::vector<unsigned char> dec((size_t)N * m, 0);
+  std::vector<unsigned char> dec((size_t)N * m, 0), declog((size_t)N * std::max(nl, 1), 0);
+  std::vector<float> cost(N, 0.0f);
   const int max_jobs = std::max(N, 1);
   std::vector<Job> jobs(max_jobs);
   alignas(16) static unsigned long long small[32];
@@ -341,6 +366,11 @@ int main(int argc, char **argv) {
   b.in = rec.data();
   b.results = res.data();
   b.dec_err = dec.data();
+  if (dem) {
+    b.in_log = logicals.data();
+    b.dec_log = declog.data();
+    b.ml_cost = variant == kMl ? cost.data() : nullptr;
+  }
   b.ncr = ncr.data();
   b.jobs = jobs.data();
   b.max_jobs = max_jobs;
@@ -373,6 +403,14 @@ int main(int argc, char **argv) {
   f = fopen((dir + "/dec.bin").c_str(), "wb");
   fwrite(dec.data(), 1, dec.size(), f);
   fclose(f);
+  if (dem) {
+    f = fopen((dir + "/declog.bin").c_str(), "wb");
+    fwrite(declog.data(), 1, (size_t)N * nl, f);
+    fclose(f);
+    f = fopen((dir + "/cost.bin").c_str(), "wb");
+    fwrite(cost.data(), sizeof(float), N, f);
+    fclose(f);
+  }
   printf("ok %d shots, %llu jobs, status %u\n", N, small[0] >> 40, status);
   return 0;
 }

@@ -1,8 +1,9 @@
 """CPU parity of the decoding kernels themselves: grand_triage.cu and
 grand_search.cu compiled for the host (tests/host_kernels.cpp: one thread block
 per kernel, one host thread per lane, warp collectives at a barrier) and run on
-CSS shots whose results must equal the oracle's in every deterministic field
-and decoded pattern.  A small light budget sends most iterations through the
+CSS and DEM shots (uniform, prob and ML searches) whose results must equal the
+oracle's in every deterministic field, decoded pattern, logical flip and ML
+cost.  A small light budget sends most iterations through the
 search kernel (run tiles, colex tiles, the Job finisher) as well as the triage
 warp's paths (empty shots, one-position iterations, bit-mask enumeration).
 Runs without a GPU."""
@@ -45,23 +46,40 @@ def _num_phases(W):  # upstream's phase count per max weight
     return {6: 2, 7: 3}.get(W, 1 if 0 < W < 6 else 0)
 
 
-def _run(exe, d, H, Ho, records, errors_input, variant, cfg, masks, light, tile_k=4):
+def _run(exe, d, H, Ho, records, errors_input, variant, cfg, masks, light, tile_k=4,
+         L=None, logicals=None, llr_path=None):
+    """CSS when L is None (Ho: the other check matrix), else DEM (L: m x n_logicos,
+    logicals: the true flips).  Returns results, decoded errors, the emulator's
+    log line and, for a DEM, decoded logical flips and ML costs."""
     W, _, _, cap, thr, mode = cfg
     n, m = H.shape
     N = records.shape[0]
+    dem = L is not None
+    nl = int(L.shape[1]) if dem else 0
+    kind = 2 if dem else (1 if errors_input else 0)
     with open(os.path.join(d, "params.txt"), "w") as f:
-        f.write(f"{variant} {1 if errors_input else 0} {n} {m} {N} {W} {mode} {thr} {cap} "
-                f"{_num_phases(W) if variant == 1 else 0} {len(masks)} {light} {tile_k}\n")
+        f.write(f"{1 if dem else 0} {variant} {kind} {n} {m} {N} {W} {mode} {thr} {cap} "
+                f"{_num_phases(W) if variant == 1 else 0} {len(masks)} {light} {tile_k} {nl}\n")
         for row in masks:
             f.write(" ".join(str(int(v)) for v in row[:4]) + "\n")
     np.ascontiguousarray(H, dtype=np.int32).tofile(os.path.join(d, "H.bin"))
-    np.ascontiguousarray(Ho, dtype=np.int32).tofile(os.path.join(d, "Hother.bin"))
     np.ascontiguousarray(records, dtype=np.int32).tofile(os.path.join(d, "rec.bin"))
+    if dem:
+        np.ascontiguousarray(L, dtype=np.int32).tofile(os.path.join(d, "L.bin"))
+        np.ascontiguousarray(logicals, dtype=np.int32).tofile(os.path.join(d, "log.bin"))
+        if llr_path:
+            shutil.copy(llr_path, os.path.join(d, "llr.txt"))
+    else:
+        np.ascontiguousarray(Ho, dtype=np.int32).tofile(os.path.join(d, "Hother.bin"))
     out = subprocess.run([exe, d], capture_output=True, text=True, timeout=600)
     assert out.returncode == 0, out.stderr + out.stdout
     res = np.fromfile(os.path.join(d, "res.bin"), dtype=capi.RESULT_DTYPE)
     dec = np.fromfile(os.path.join(d, "dec.bin"), dtype=np.uint8).reshape(N, m)
-    return res, dec, out.stdout
+    if not dem:
+        return res, dec, out.stdout
+    dlog = np.fromfile(os.path.join(d, "declog.bin"), dtype=np.uint8).reshape(N, nl)
+    cost = np.fromfile(os.path.join(d, "cost.bin"), dtype=np.float32)
+    return res, dec, out.stdout, dlog, cost
 
 
 def _compare(res, dec, pres, pdec):
@@ -100,3 +118,27 @@ def test_prob_syndromes(emulator, port, tmp_path):
     assert prc == 0
     _compare(res, dec, pres, pdec)
     assert int(log.split()[3]) > 0, log  # the search kernel had Jobs
+
+
+@pytest.mark.parametrize("variant", ["uniform", "prob", "ml"])
+def test_dem(emulator, port, tmp_path, variant):
+    dem = synth.random_dem(8, detectors=48, mechanisms=200, logicals=6, p_range=(4e-3, 3e-2))
+    det, log, _ = synth.dem_shots(dem, 160, seed=990)
+    cfg = (3, 256, 0, 24, 10, -1)
+    masks, path, v, pv = [], None, 0, O.UNIFORM
+    if variant == "prob":
+        masks = [(5, 0, 1, 2, 0.7, 0.2, 0.1), (300, 0, 1, 2, 0.6, 0.3, 0.1)]
+        path, v, pv = synth.write_phase_file(str(tmp_path / "phase.txt"), masks), 1, O.PROB
+    elif variant == "ml":
+        path, v, pv = synth.write_llr_file(str(tmp_path / "llr.txt"), dem.llr), 2, O.ML
+    d = tmp_path / "run"
+    d.mkdir()
+    res, dec, out, dlog, cost = _run(emulator, str(d), dem.h, None, det, False, v, cfg, masks, 3,
+                                     L=dem.l, logicals=log, llr_path=path if v == 2 else None)
+    prc, pres, pdec, pdlog, pcost = port.dem(pv, dem.h, dem.l, det, log, O.Config(*cfg), path)
+    assert prc == 0
+    _compare(res, dec, pres, pdec)
+    assert np.array_equal(dlog, pdlog)
+    if variant == "ml":
+        assert np.array_equal(cost.view(np.uint32), np.asarray(pcost, np.float32).view(np.uint32))
+    assert int(out.split()[3]) > 0, out  # the search kernel had Jobs
