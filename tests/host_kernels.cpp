@@ -242,9 +242,11 @@ int main(int argc, char **argv) {
   const std::string dir = argv[1];
   FILE *pf = fopen((dir + "/params.txt").c_str(), "r");
   if (!pf) return 2;
-  int family, variant, input_kind, n, m, N, W, mode, thr, cap, num_phases, n_masks, light, tile_k, nl;
-  if (fscanf(pf, "%d %d %d %d %d %d %d %d %d %d %d %d %d %d %d", &family, &variant, &input_kind, &n,
-             &m, &N, &W, &mode, &thr, &cap, &num_phases, &n_masks, &light, &tile_k, &nl) != 15)
+  int family, variant, input_kind, n, m, N, W, mode, thr, cap, num_phases, n_masks, light, tile_k, nl,
+      packed;
+  if (fscanf(pf, "%d %d %d %d %d %d %d %d %d %d %d %d %d %d %d %d", &family, &variant, &input_kind,
+             &n, &m, &N, &W, &mode, &thr, &cap, &num_phases, &n_masks, &light, &tile_k, &nl,
+             &packed) != 16)
     return 2;
   DevCode d;
   memset(&d, 0, sizeof(d));
@@ -257,10 +259,13 @@ int main(int argc, char **argv) {
   const std::vector<int> H = read_ints(dir + "/H.bin", (size_t)n * m);
   const std::vector<int> Ho = dem ? std::vector<int>() : read_ints(dir + "/Hother.bin", (size_t)n * m);
   const std::vector<int> L = dem ? read_ints(dir + "/L.bin", (size_t)m * nl) : std::vector<int>();
-  const int rec_len = input_kind == kInErrors ? m : n;
+  // records: one int32 per entry, or LSB-first uint32 words when packed
+  const int entries = input_kind == kInErrors ? m : n;
+  const int rec_len = packed ? (entries + 31) / 32 : entries;
   const std::vector<int> rec = read_ints(dir + "/rec.bin", (size_t)N * rec_len);
+  const int log_len = packed ? (nl + 31) / 32 : nl;
   const std::vector<int> logicals =
-      dem ? read_ints(dir + "/log.bin", (size_t)N * std::max(nl, 1)) : std::vector<int>();
+      dem ? read_ints(dir + "/log.bin", (size_t)N * std::max(log_len, 1)) : std::vector<int>();
   std::vector<float> llr(m, 0.0f);
   if (variant == kMl) {  // the library's reader: fscanf("%f") per column
     FILE *lf = fopen((dir + "/llr.txt").c_str(), "r");
@@ -338,6 +343,7 @@ int main(int argc, char **argv) {
   d.n_masks = n_masks;
   d.rank = rank;
   d.rec_len = rec_len;
+  d.packed = packed;
   d.cols = cols.data();
   d.colw = colw.data();
   d.rref = rows.data();

@@ -47,7 +47,7 @@ def _num_phases(W):  # upstream's phase count per max weight
 
 
 def _run(exe, d, H, Ho, records, errors_input, variant, cfg, masks, light, tile_k=4,
-         L=None, logicals=None, llr_path=None):
+         L=None, logicals=None, llr_path=None, packed=False):
     """CSS when L is None (Ho: the other check matrix), else DEM (L: m x n_logicos,
     logicals: the true flips).  Returns results, decoded errors, the emulator's
     log line and, for a DEM, decoded logical flips and ML costs."""
@@ -59,14 +59,16 @@ def _run(exe, d, H, Ho, records, errors_input, variant, cfg, masks, light, tile_
     kind = 2 if dem else (1 if errors_input else 0)
     with open(os.path.join(d, "params.txt"), "w") as f:
         f.write(f"{1 if dem else 0} {variant} {kind} {n} {m} {N} {W} {mode} {thr} {cap} "
-                f"{_num_phases(W) if variant == 1 else 0} {len(masks)} {light} {tile_k} {nl}\n")
+                f"{_num_phases(W) if variant == 1 else 0} {len(masks)} {light} {tile_k} {nl} "
+                f"{1 if packed else 0}\n")
         for row in masks:
             f.write(" ".join(str(int(v)) for v in row[:4]) + "\n")
     np.ascontiguousarray(H, dtype=np.int32).tofile(os.path.join(d, "H.bin"))
-    np.ascontiguousarray(records, dtype=np.int32).tofile(os.path.join(d, "rec.bin"))
+    pack = (lambda a: capi.pack_bits(a)) if packed else (lambda a: np.asarray(a, dtype=np.int32))
+    np.ascontiguousarray(pack(records)).tofile(os.path.join(d, "rec.bin"))
     if dem:
         np.ascontiguousarray(L, dtype=np.int32).tofile(os.path.join(d, "L.bin"))
-        np.ascontiguousarray(logicals, dtype=np.int32).tofile(os.path.join(d, "log.bin"))
+        np.ascontiguousarray(pack(logicals)).tofile(os.path.join(d, "log.bin"))
         if llr_path:
             shutil.copy(llr_path, os.path.join(d, "llr.txt"))
     else:
@@ -89,21 +91,26 @@ def _compare(res, dec, pres, pdec):
     assert len(diff) == 0, f"decoded patterns differ on shots {diff[:5]}"
 
 
-@pytest.mark.parametrize("W,mode,thr,cap,light", [(4, -1, 10, 64, 3), (3, 0, 10, 64, 5),
-                                                  (4, 1, 8, 24, 12), (5, -1, 10, 64, 4)])
-def test_uniform_errors(emulator, port, tmp_path, W, mode, thr, cap, light):
+@pytest.mark.parametrize("W,mode,thr,cap,light,packed", [(4, -1, 10, 64, 3, False),
+                                                         (4, -1, 10, 64, 3, True),
+                                                         (3, 0, 10, 64, 5, False),
+                                                         (4, 1, 8, 24, 12, False),
+                                                         (5, -1, 10, 64, 4, False)])
+def test_uniform_errors(emulator, port, tmp_path, W, mode, thr, cap, light, packed):
     code = synth.BB_CODES[72]()
     errors = np.concatenate([synth.css_shots(code.hz, 60, p, seed=900 + i)[0]
                              for i, p in enumerate((0.01, 0.03, 0.06))])
     cfg = (W, 256, 0, cap, thr, mode)
-    res, dec, log = _run(emulator, str(tmp_path), code.hz, code.hx, errors, True, 0, cfg, [], light)
+    res, dec, log = _run(emulator, str(tmp_path), code.hz, code.hx, errors, True, 0, cfg, [], light,
+                         packed=packed)
     prc, pres, pdec = port.css(O.UNIFORM, code.hx, code.hz, errors, None, O.Config(*cfg), "x")
     assert prc == 0
     _compare(res, dec, pres, pdec)
     assert int(log.split()[3]) > 0 or light >= 12, log  # the search kernel had Jobs
 
 
-def test_prob_syndromes(emulator, port, tmp_path):
+@pytest.mark.parametrize("packed", [False, True])
+def test_prob_syndromes(emulator, port, tmp_path, packed):
     code = synth.BB_CODES[108]()
     errors = np.concatenate([synth.css_shots(code.hz, 60, p, seed=950 + i)[0]
                              for i, p in enumerate((0.01, 0.03))])
@@ -113,15 +120,17 @@ def test_prob_syndromes(emulator, port, tmp_path):
     cfg = (4, 256, 0, 30, 8, 1)  # mode 1: sets above 30 positions are skipped
     d = tmp_path / "run"
     d.mkdir()
-    res, dec, log = _run(emulator, str(d), code.hz, code.hx, syn, False, 1, cfg, masks, 4)
+    res, dec, log = _run(emulator, str(d), code.hz, code.hx, syn, False, 1, cfg, masks, 4,
+                         packed=packed)
     prc, pres, pdec = port.css(O.PROB, code.hx, code.hz, None, syn, O.Config(*cfg), "x", phase)
     assert prc == 0
     _compare(res, dec, pres, pdec)
     assert int(log.split()[3]) > 0, log  # the search kernel had Jobs
 
 
-@pytest.mark.parametrize("variant", ["uniform", "prob", "ml"])
-def test_dem(emulator, port, tmp_path, variant):
+@pytest.mark.parametrize("variant,packed", [("uniform", False), ("prob", False), ("ml", False),
+                                            ("ml", True)])
+def test_dem(emulator, port, tmp_path, variant, packed):
     dem = synth.random_dem(8, detectors=48, mechanisms=200, logicals=6, p_range=(4e-3, 3e-2))
     det, log, _ = synth.dem_shots(dem, 160, seed=990)
     cfg = (3, 256, 0, 24, 10, -1)
@@ -134,7 +143,8 @@ def test_dem(emulator, port, tmp_path, variant):
     d = tmp_path / "run"
     d.mkdir()
     res, dec, out, dlog, cost = _run(emulator, str(d), dem.h, None, det, False, v, cfg, masks, 3,
-                                     L=dem.l, logicals=log, llr_path=path if v == 2 else None)
+                                     L=dem.l, logicals=log, llr_path=path if v == 2 else None,
+                                     packed=packed)
     prc, pres, pdec, pdlog, pcost = port.dem(pv, dem.h, dem.l, det, log, O.Config(*cfg), path)
     assert prc == 0
     _compare(res, dec, pres, pdec)
