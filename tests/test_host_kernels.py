@@ -152,3 +152,21 @@ def test_dem(emulator, port, tmp_path, variant, packed):
     if variant == "ml":
         assert np.array_equal(cost.view(np.uint32), np.asarray(pcost, np.float32).view(np.uint32))
     assert int(out.split()[3]) > 0, out  # the search kernel had Jobs
+
+
+def test_wide_rows_and_weight_six(emulator, port, tmp_path):
+    # BB[[288]]: 144 check rows, so a column spans 5 words (8 with padding) and the
+    # flagged-check counts take their general path; prob with W = 7 lists phase 1
+    # (weight 6) and phase 2, in orders that differ by active-set size
+    code = synth.BB_CODES[288]()
+    errors = np.concatenate([synth.css_shots(code.hz, 40, p, seed=970 + i)[0]
+                             for i, p in enumerate((0.004, 0.01))])
+    masks = [(6, 1, 0, 2, 0.2, 0.7, 0.1), (300, 0, 2, 1, 0.8, 0.1, 0.1)]
+    phase = synth.write_phase_file(str(tmp_path / "phase.txt"), masks)
+    cfg = (7, 256, 0, 12, 6, 1)  # mode 1 and cap 12 keep the weight-6 blocks small
+    d = tmp_path / "run"
+    d.mkdir()
+    res, dec, log = _run(emulator, str(d), code.hz, code.hx, errors, True, 1, cfg, masks, 3)
+    prc, pres, pdec = port.css(O.PROB, code.hx, code.hz, errors, None, O.Config(*cfg), "x", phase)
+    assert prc == 0
+    _compare(res, dec, pres, pdec)
