@@ -14,7 +14,8 @@
 // a DEM, DIR/L.bin (m x n_logicos) and DIR/log.bin (true logical flips), plus
 // DIR/llr.txt for ML; writes DIR/res.bin (72-byte results), DIR/dec.bin (decoded
 // errors, a byte per column and shot) and, for a DEM, DIR/declog.bin (decoded
-// logical flips) and DIR/cost.bin (ML costs, FP32).
+// logical flips) and DIR/cost.bin (ML costs, FP32).  With DIR/mixed.txt it runs
+// one batch that mixes several codes instead (see main).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -237,84 +238,93 @@ static unsigned long long C(int n, int k) {
   return r;
 }
 
-int main(int argc, char **argv) {
-  if (argc != 2) return 2;
-  const std::string dir = argv[1];
-  FILE *pf = fopen((dir + "/params.txt").c_str(), "r");
-  if (!pf) return 2;
-  int family, variant, input_kind, n, m, N, W, mode, thr, cap, num_phases, n_masks, light, tile_k, nl,
-      packed;
-  if (fscanf(pf, "%d %d %d %d %d %d %d %d %d %d %d %d %d %d %d %d", &family, &variant, &input_kind,
-             &n, &m, &N, &W, &mode, &thr, &cap, &num_phases, &n_masks, &light, &tile_k, &nl,
-             &packed) != 16)
-    return 2;
+// One code: its parameters (DIR/params.txt), its matrices and, for ML, its LLRs,
+// with the code tables built as the library builds them.
+struct Code {
+  int family = 0, variant = 0, input_kind = 0, n = 0, m = 0, N = 0, W = 0, nl = 0, packed = 0;
+  int light = 12, tile_k = 4, rec_len = 0, log_len = 0;
+  std::vector<uint32_t> cols, hcol, rows, lcols;
+  std::vector<int> colw, pivrow;
+  std::vector<float> llr;
   DevCode d;
+};
+
+static bool load_code(const std::string &dir, Code &k) {
+  FILE *pf = fopen((dir + "/params.txt").c_str(), "r");
+  if (!pf) return false;
+  int mode, thr, cap, num_phases, n_masks;
+  if (fscanf(pf, "%d %d %d %d %d %d %d %d %d %d %d %d %d %d %d %d", &k.family, &k.variant,
+             &k.input_kind, &k.n, &k.m, &k.N, &k.W, &mode, &thr, &cap, &num_phases, &n_masks,
+             &k.light, &k.tile_k, &k.nl, &k.packed) != 16)
+    return false;
+  DevCode &d = k.d;
   memset(&d, 0, sizeof(d));
   for (int q = 0; q < n_masks; ++q)
     if (fscanf(pf, "%d %d %d %d", &d.mask_tam_upper[q], &d.mask_order[q][0], &d.mask_order[q][1],
                &d.mask_order[q][2]) != 4)
-      return 2;
+      return false;
   fclose(pf);
-  const bool dem = family == kDem;
+  const int n = k.n, m = k.m, nl = k.nl;
+  const bool dem = k.family == kDem;
   const std::vector<int> H = read_ints(dir + "/H.bin", (size_t)n * m);
   const std::vector<int> Ho = dem ? std::vector<int>() : read_ints(dir + "/Hother.bin", (size_t)n * m);
   const std::vector<int> L = dem ? read_ints(dir + "/L.bin", (size_t)m * nl) : std::vector<int>();
   // records: one int32 per entry, or LSB-first uint32 words when packed
-  const int entries = input_kind == kInErrors ? m : n;
-  const int rec_len = packed ? (entries + 31) / 32 : entries;
-  const std::vector<int> rec = read_ints(dir + "/rec.bin", (size_t)N * rec_len);
-  const int log_len = packed ? (nl + 31) / 32 : nl;
-  const std::vector<int> logicals =
-      dem ? read_ints(dir + "/log.bin", (size_t)N * std::max(log_len, 1)) : std::vector<int>();
-  std::vector<float> llr(m, 0.0f);
-  if (variant == kMl) {  // the library's reader: fscanf("%f") per column
+  const int entries = k.input_kind == kInErrors ? m : n;
+  k.rec_len = k.packed ? (entries + 31) / 32 : entries;
+  k.log_len = k.packed ? (nl + 31) / 32 : nl;
+  k.llr.assign(m, 0.0f);
+  if (k.variant == kMl) {  // the library's reader: fscanf("%f") per column
     FILE *lf = fopen((dir + "/llr.txt").c_str(), "r");
-    if (!lf) return 2;
+    if (!lf) return false;
     for (int i = 0; i < m; ++i)
-      if (fscanf(lf, "%f", &llr[i]) != 1) return 2;
+      if (fscanf(lf, "%f", &k.llr[i]) != 1) return false;
     fclose(lf);
   }
-
-  // code tables, built as the library builds them for a CSS code
   const int nw = (n + 31) / 32;
   const int nwp = nw <= 2 ? nw : (nw <= 4 ? 4 : (nw <= 8 ? 8 : (nw + 3) & ~3));
   const int mw = (m + 31) / 32;
-  std::vector<uint32_t> cols((size_t)m * nwp, 0u), hcol(m, 0u);
-  std::vector<int> colw(m, 0);
+  k.cols.assign((size_t)m * nwp, 0u);
+  k.hcol.assign(m, 0u);
+  k.colw.assign(m, 0);
   for (int r = 0; r < n; ++r)
     for (int c = 0; c < m; ++c)
       if (H[(size_t)r * m + c] != 0) {
-        ++colw[c];
-        cols[(size_t)c * nwp + (r >> 5)] |= 1u << (r & 31);
-        hcol[c] ^= row_hash(r);
+        ++k.colw[c];
+        k.cols[(size_t)c * nwp + (r >> 5)] |= 1u << (r & 31);
+        k.hcol[c] ^= row_hash(r);
       }
   int max_soma = 0, regular = 1;
-  for (int c = 0; c < m; ++c) max_soma = std::max(max_soma, colw[c]);
+  for (int c = 0; c < m; ++c) max_soma = std::max(max_soma, k.colw[c]);
   for (int c = 1; c < m; ++c)
-    if (colw[c] != colw[0]) regular = 0;
-  std::vector<uint32_t> rows(dem ? 0 : (size_t)n * mw, 0u);
+    if (k.colw[c] != k.colw[0]) regular = 0;
+  k.rows.assign(dem ? 0 : (size_t)n * mw, 0u);
   for (int r = 0; r < n && !dem; ++r)
     for (int c = 0; c < m; ++c)
-      if (Ho[(size_t)r * m + c] & 1) rows[(size_t)r * mw + (c >> 5)] |= 1u << (c & 31);
-  std::vector<int> pivrow(m, -1);
+      if (Ho[(size_t)r * m + c] & 1) k.rows[(size_t)r * mw + (c >> 5)] |= 1u << (c & 31);
+  k.pivrow.assign(m, -1);
   int rank = 0;
   for (int c = 0; c < m && rank < n && !dem; ++c) {  // reduced row echelon form over GF(2)
     const int q = c >> 5;
     const uint32_t bit = 1u << (c & 31);
     int p = -1;
     for (int i = rank; i < n; ++i)
-      if (rows[(size_t)i * mw + q] & bit) {
+      if (k.rows[(size_t)i * mw + q] & bit) {
         p = i;
         break;
       }
     if (p < 0) continue;
-    for (int j = 0; j < mw; ++j) std::swap(rows[(size_t)rank * mw + j], rows[(size_t)p * mw + j]);
+    for (int j = 0; j < mw; ++j) std::swap(k.rows[(size_t)rank * mw + j], k.rows[(size_t)p * mw + j]);
     for (int i = 0; i < n; ++i)
-      if (i != rank && (rows[(size_t)i * mw + q] & bit))
-        for (int j = 0; j < mw; ++j) rows[(size_t)i * mw + j] ^= rows[(size_t)rank * mw + j];
-    pivrow[c] = rank++;
+      if (i != rank && (k.rows[(size_t)i * mw + q] & bit))
+        for (int j = 0; j < mw; ++j) k.rows[(size_t)i * mw + j] ^= k.rows[(size_t)rank * mw + j];
+    k.pivrow[c] = rank++;
   }
-
+  const int nlw = (nl + 31) / 32;
+  k.lcols.assign((size_t)m * std::max(nlw, 1), 0u);
+  for (int c = 0; c < m && dem; ++c)
+    for (int j = 0; j < nl; ++j)
+      if (L[(size_t)c * nl + j] != 0) k.lcols[(size_t)c * nlw + (j >> 5)] |= 1u << (j & 31);
   d.R = n;
   d.m = m;
   d.nw = nw;
@@ -322,61 +332,56 @@ int main(int argc, char **argv) {
   d.mw = mw;
   d.max_soma = max_soma;
   d.regular = regular;
-  const int nlw = (nl + 31) / 32;
-  std::vector<uint32_t> lcols((size_t)m * std::max(nlw, 1), 0u);
-  for (int c = 0; c < m && dem; ++c)
-    for (int j = 0; j < nl; ++j)
-      if (L[(size_t)c * nl + j] != 0) lcols[(size_t)c * nlw + (j >> 5)] |= 1u << (j & 31);
   d.family = dem ? kDem : kCss;
   d.n_logicos = nl;
   d.nlw = nlw;
-  d.lcols = lcols.data();
-  d.llr = llr.data();
-  d.variant = variant;
-  d.input_kind = input_kind;
-  d.W = W;
-  d.Wc = std::min(W, (int)kMaxW);
+  d.lcols = k.lcols.data();
+  d.llr = k.llr.data();
+  d.variant = k.variant;
+  d.input_kind = k.input_kind;
+  d.W = k.W;
+  d.Wc = std::min(k.W, (int)kMaxW);
   d.mode = mode;
   d.thr = thr;
   d.cap = cap;
   d.num_phases = num_phases;
   d.n_masks = n_masks;
   d.rank = rank;
-  d.rec_len = rec_len;
-  d.packed = packed;
-  d.cols = cols.data();
-  d.colw = colw.data();
-  d.rref = rows.data();
-  d.pivrow = pivrow.data();
-  d.hcol = hcol.data();
+  d.rec_len = k.rec_len;
+  d.packed = k.packed;
+  d.cols = k.cols.data();
+  d.colw = k.colw.data();
+  d.rref = k.rows.data();
+  d.pivrow = k.pivrow.data();
+  d.hcol = k.hcol.data();
+  return true;
+}
 
-  std::vector<unsigned long long> ncr((size_t)(kMaxTam + 1) * (kMaxW + 1));
-  for (int a = 0; a <= kMaxTam; ++a)
-    for (int k = 0; k <= kMaxW; ++k) ncr[(size_t)a * (kMaxW + 1) + k] = C(a, k);
-  std::vector<GrandDecoderResult> res(N);
-  std::vector<unsigned char> dec((size_t)N * m, 0), declog((size_t)N * std::max(nl, 1), 0);
-  std::vector<float> cost(N, 0.0f);
+static void write_bytes(const std::string &path, const void *p, size_t n) {
+  FILE *f = fopen(path.c_str(), "wb");
+  fwrite(p, 1, n, f);
+  fclose(f);
+}
+
+// Both kernels over a batch, as the library launches them (counters zeroed).
+static unsigned run_batch(DevBatch &b, int N) {
+  static std::vector<unsigned long long> ncr;
+  if (ncr.empty()) {
+    ncr.resize((size_t)(kMaxTam + 1) * (kMaxW + 1));
+    for (int a = 0; a <= kMaxTam; ++a)
+      for (int k = 0; k <= kMaxW; ++k) ncr[(size_t)a * (kMaxW + 1) + k] = C(a, k);
+  }
   const int max_jobs = std::max(N, 1);
-  std::vector<Job> jobs(max_jobs);
+  static std::vector<Job> jobs;
+  jobs.assign(max_jobs, Job());
   alignas(16) static unsigned long long small[32];
   memset(small, 0, sizeof(small));
   const unsigned long long scratch_words = 8ull << 20;
-  std::vector<uint32_t> scratch(scratch_words);
-  std::vector<int> deferred(N, 0);
-
-  DevBatch b;
-  memset(&b, 0, sizeof(b));
+  static std::vector<uint32_t> scratch;
+  scratch.assign(scratch_words, 0u);
+  static std::vector<int> deferred;
+  deferred.assign(N, 0);
   b.num_shots = N;
-  b.num_codes = 1;
-  b.codes = &d;
-  b.in = rec.data();
-  b.results = res.data();
-  b.dec_err = dec.data();
-  if (dem) {
-    b.in_log = logicals.data();
-    b.dec_log = declog.data();
-    b.ml_cost = variant == kMl ? cost.data() : nullptr;
-  }
   b.ncr = ncr.data();
   b.jobs = jobs.data();
   b.max_jobs = max_jobs;
@@ -385,10 +390,6 @@ int main(int argc, char **argv) {
   b.scratch = scratch.data();
   b.scratch_words = scratch_words;
   b.deferred = deferred.data();
-  b.light_max_log2 = light;
-  b.tile_k = tile_k;
-  b.has_ml = variant == kMl;
-
   run_block(kTriageWarps * 32, [&] {
     if (b.has_ml) triage_kernel<true>(b);
     else triage_kernel<false>(b);
@@ -397,26 +398,89 @@ int main(int argc, char **argv) {
     if (b.has_ml) search_kernel<true>(b);
     else search_kernel<false>(b);
   });
-  const unsigned status = *b.status;
   for (int i = 0; i < N; ++i)
     if (deferred[i]) {
-      fprintf(stderr, "shot %d deferred (status %u)\n", i, status);
-      return 3;
+      fprintf(stderr, "shot %d deferred (status %u)\n", i, *b.status);
+      exit(3);
     }
-  FILE *f = fopen((dir + "/res.bin").c_str(), "wb");
-  fwrite(res.data(), sizeof(GrandDecoderResult), N, f);
-  fclose(f);
-  f = fopen((dir + "/dec.bin").c_str(), "wb");
-  fwrite(dec.data(), 1, dec.size(), f);
-  fclose(f);
-  if (dem) {
-    f = fopen((dir + "/declog.bin").c_str(), "wb");
-    fwrite(declog.data(), 1, (size_t)N * nl, f);
-    fclose(f);
-    f = fopen((dir + "/cost.bin").c_str(), "wb");
-    fwrite(cost.data(), sizeof(float), N, f);
-    fclose(f);
+  printf("ok %d shots, %llu jobs, status %u\n", N, small[0] >> 40, *b.status);
+  return *b.status;
+}
+
+int main(int argc, char **argv) {
+  if (argc != 2) return 2;
+  const std::string dir = argv[1];
+  DevBatch b;
+  memset(&b, 0, sizeof(b));
+
+  // a mixed batch: DIR/mixed.txt = "K N light tile_k", codes in DIR/code<k>/, the
+  // shots' records back to back in DIR/rec.bin with DIR/off.bin (int64 start of
+  // each record) and DIR/code.bin (int32 code of each shot); results only
+  if (FILE *mf = fopen((dir + "/mixed.txt").c_str(), "r")) {
+    int K, N, light, tile_k;
+    if (fscanf(mf, "%d %d %d %d", &K, &N, &light, &tile_k) != 4) return 2;
+    fclose(mf);
+    std::vector<Code> codes(K);
+    std::vector<DevCode> dcs(K);
+    for (int k = 0; k < K; ++k) {
+      if (!load_code(dir + "/code" + std::to_string(k), codes[k])) return 2;
+      dcs[k] = codes[k].d;
+      b.has_ml |= codes[k].variant == kMl;
+    }
+    FILE *rf = fopen((dir + "/rec.bin").c_str(), "rb");
+    if (!rf) return 2;
+    fseek(rf, 0, SEEK_END);
+    const size_t total = (size_t)ftell(rf) / 4;
+    fclose(rf);
+    const std::vector<int> rec = read_ints(dir + "/rec.bin", total);
+    std::vector<long long> off(N);
+    FILE *of = fopen((dir + "/off.bin").c_str(), "rb");
+    if (!of || fread(off.data(), 8, N, of) != (size_t)N) return 2;
+    fclose(of);
+    const std::vector<int> shot_code = read_ints(dir + "/code.bin", N);
+    std::vector<GrandDecoderResult> res(N);
+    b.num_codes = K;
+    b.codes = dcs.data();
+    b.in = rec.data();
+    b.in_off = off.data();
+    b.shot_code = shot_code.data();
+    b.results = res.data();
+    b.light_max_log2 = light;
+    b.tile_k = tile_k;
+    run_batch(b, N);
+    write_bytes(dir + "/res.bin", res.data(), sizeof(GrandDecoderResult) * N);
+    return 0;
   }
-  printf("ok %d shots, %llu jobs, status %u\n", N, small[0] >> 40, status);
+
+  Code k;
+  if (!load_code(dir, k)) return 2;
+  const int N = k.N, m = k.m, nl = k.nl;
+  const bool dem = k.family == kDem;
+  const std::vector<int> rec = read_ints(dir + "/rec.bin", (size_t)N * k.rec_len);
+  const std::vector<int> logicals =
+      dem ? read_ints(dir + "/log.bin", (size_t)N * std::max(k.log_len, 1)) : std::vector<int>();
+  std::vector<GrandDecoderResult> res(N);
+  std::vector<unsigned char> dec((size_t)N * m, 0), declog((size_t)N * std::max(nl, 1), 0);
+  std::vector<float> cost(N, 0.0f);
+  b.num_codes = 1;
+  b.codes = &k.d;
+  b.in = rec.data();
+  b.results = res.data();
+  b.dec_err = dec.data();
+  if (dem) {
+    b.in_log = logicals.data();
+    b.dec_log = declog.data();
+    b.ml_cost = k.variant == kMl ? cost.data() : nullptr;
+  }
+  b.light_max_log2 = k.light;
+  b.tile_k = k.tile_k;
+  b.has_ml = k.variant == kMl;
+  run_batch(b, N);
+  write_bytes(dir + "/res.bin", res.data(), sizeof(GrandDecoderResult) * N);
+  write_bytes(dir + "/dec.bin", dec.data(), dec.size());
+  if (dem) {
+    write_bytes(dir + "/declog.bin", declog.data(), (size_t)N * nl);
+    write_bytes(dir + "/cost.bin", cost.data(), sizeof(float) * N);
+  }
   return 0;
 }

@@ -170,3 +170,67 @@ def test_wide_rows_and_weight_six(emulator, port, tmp_path):
     prc, pres, pdec = port.css(O.PROB, code.hx, code.hz, errors, None, O.Config(*cfg), "x", phase)
     assert prc == 0
     _compare(res, dec, pres, pdec)
+
+
+def _write_code(d, H, variant, kind, cfg, masks, Ho=None, L=None, llr_path=None):
+    os.makedirs(d)
+    W, _, _, cap, thr, mode = cfg
+    n, m = H.shape
+    nl = 0 if L is None else int(L.shape[1])
+    with open(os.path.join(d, "params.txt"), "w") as f:
+        f.write(f"{0 if L is None else 1} {variant} {kind} {n} {m} 0 {W} {mode} {thr} {cap} "
+                f"{_num_phases(W) if variant == 1 else 0} {len(masks)} 0 0 {nl} 0\n")
+        for row in masks:
+            f.write(" ".join(str(int(v)) for v in row[:4]) + "\n")
+    np.ascontiguousarray(H, dtype=np.int32).tofile(os.path.join(d, "H.bin"))
+    if L is None:
+        np.ascontiguousarray(Ho, dtype=np.int32).tofile(os.path.join(d, "Hother.bin"))
+    else:
+        np.ascontiguousarray(L, dtype=np.int32).tofile(os.path.join(d, "L.bin"))
+    if llr_path:
+        shutil.copy(llr_path, os.path.join(d, "llr.txt"))
+
+
+def test_mixed_codes_in_one_batch(emulator, port, tmp_path):
+    """Three codes in one shuffled batch (per-shot code and record offsets, as the
+    engine launches them): each shot's result equals the oracle's for its code."""
+    c72, c108 = synth.BB_CODES[72](), synth.BB_CODES[108]()
+    dem = synth.random_dem(4, detectors=40, mechanisms=160, logicals=5, p_range=(4e-3, 3e-2))
+    e72 = synth.css_shots(c72.hz, 70, 0.03, seed=31)[0]
+    e108 = synth.css_shots(c108.hz, 70, 0.02, seed=32)[0]
+    s108 = (e108.astype(np.int64) @ c108.hz.T.astype(np.int64) % 2).astype(np.int32)
+    det, log, _ = synth.dem_shots(dem, 70, seed=33)
+    masks = [(8, 0, 1, 2, 0.6, 0.3, 0.1), (300, 0, 1, 2, 0.6, 0.3, 0.1)]
+    phase = synth.write_phase_file(str(tmp_path / "phase.txt"), masks)
+    llr = synth.write_llr_file(str(tmp_path / "llr.txt"), dem.llr)
+    cfg72, cfg108, cfgd = (3, 256, 0, 64, 10, -1), (4, 256, 0, 30, 8, 1), (3, 256, 0, 24, 10, -1)
+    d = tmp_path / "mix"
+    _write_code(str(d / "code0"), c72.hz, 0, 1, cfg72, [], Ho=c72.hx)
+    _write_code(str(d / "code1"), c108.hz, 1, 0, cfg108, masks, Ho=c108.hx)
+    _write_code(str(d / "code2"), dem.h, 2, 2, cfgd, [], L=dem.l, llr_path=llr)
+    records = [list(r) for r in e72] + [list(r) for r in s108] + \
+              [list(a) + list(b) for a, b in zip(det, log)]  # DEM: detectors, then logicals
+    codes = [0] * 70 + [1] * 70 + [2] * 70
+    order = np.random.default_rng(34).permutation(len(records))
+    flat, off = [], []
+    for i in order:
+        off.append(len(flat))
+        flat.extend(records[i])
+    N = len(order)
+    with open(d / "mixed.txt", "w") as f:
+        f.write(f"3 {N} 3 4\n")
+    np.asarray(flat, dtype=np.int32).tofile(d / "rec.bin")
+    np.asarray(off, dtype=np.int64).tofile(d / "off.bin")
+    np.asarray([codes[i] for i in order], dtype=np.int32).tofile(d / "code.bin")
+    out = subprocess.run([emulator, str(d)], capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr + out.stdout
+    res = np.fromfile(d / "res.bin", dtype=capi.RESULT_DTYPE)
+    assert int(out.stdout.split()[3]) > 0, out.stdout  # the search kernel had Jobs
+    got = np.empty(N, dtype=capi.RESULT_DTYPE)
+    got[order] = res  # back to the per-code order
+    _, p72, _ = port.css(O.UNIFORM, c72.hx, c72.hz, e72, None, O.Config(*cfg72), "x")
+    _, p108, _ = port.css(O.PROB, c108.hx, c108.hz, None, s108, O.Config(*cfg108), "x", phase)
+    _, pd, _, _, _ = port.dem(O.ML, dem.h, dem.l, det, log, O.Config(*cfgd), llr)
+    for part, want in ((got[:70], p72), (got[70:140], p108), (got[140:], pd)):
+        bad = O.fields_equal(part, want)
+        assert len(bad) == 0, f"shots {bad[:5]}\nemulated {part[bad[:3]]}\noracle {want[bad[:3]]}"
