@@ -234,3 +234,31 @@ def test_mixed_codes_in_one_batch(emulator, port, tmp_path):
     for part, want in ((got[:70], p72), (got[70:140], p108), (got[140:], pd)):
         bad = O.fields_equal(part, want)
         assert len(bad) == 0, f"shots {bad[:5]}\nemulated {part[bad[:3]]}\noracle {want[bad[:3]]}"
+
+
+def test_largest_code_shapes(emulator, port, tmp_path):
+    """The kernels' size limits: 1024 check rows (every lane of the warp holds a
+    syndrome word) and 4000 columns (125 mask words per threshold iteration);
+    syndromes of one or two columns, empty ones and random dense ones, with
+    mode 1 and a cap that skip the dense shots' large active sets; three- and
+    four-column syndromes (beyond W = 2) become Jobs for the search kernel."""
+    rng = np.random.default_rng(77)
+    n, m = 1024, 4000
+    hz = np.zeros((n, m), dtype=np.int32)
+    for c in range(m):
+        hz[rng.choice(n, 3, replace=False), c] = 1
+    hx = np.zeros((n, m), dtype=np.int32)  # unused by syndrome records
+    syn = np.zeros((100, n), dtype=np.int32)
+    for i in range(80):  # 1-2 columns (found), then 3-4 (beyond W: searched to the end)
+        for c in rng.choice(m, 1 + i % 2 if i < 60 else 3 + i % 2, replace=False):
+            syn[i] ^= hz[:, c]
+    syn[90:] = rng.integers(0, 2, size=(10, n))
+    cfg = (2, 256, 0, 40, 10, 1)
+    d = tmp_path / "run"
+    d.mkdir()
+    res, dec, log = _run(emulator, str(d), hz, hx, syn, False, 0, cfg, [], 3)
+    prc, pres, pdec = port.css(O.UNIFORM, hx, hz, None, syn, O.Config(*cfg), "x")
+    assert prc == 0
+    _compare(res, dec, pres, pdec)
+    assert int((pres["found"] == 1).sum()) >= 55
+    assert int(log.split()[3]) > 0, log  # the search kernel had Jobs
