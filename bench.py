@@ -46,12 +46,10 @@ FLUSH_BYTES = 256 << 20
 
 
 def workload(seed: int):
-    from library_s_grand_gb300 import synth
-    code = synth.BB_CODES[144]()
-    rng = np.random.default_rng(0)
-    p = np.exp(rng.uniform(np.log(1e-3), np.log(1e-2), code.m))
-    errors, _ = synth.css_shots(code.hz, SHOTS, p, seed=1 + seed)
-    return code, errors
+    """The headline batch for one rank (seed 0 on rank 0; other ranks draw other shots)."""
+    from library_s_grand_gb300 import workloads
+    w = workloads.prob_bb144(seed)
+    return w.code, w.errors
 
 
 def workload_config():
@@ -66,74 +64,105 @@ def workload_config():
 # CPU side: the upstream CPU search algorithm on host cores
 # ---------------------------------------------------------------------------
 _W = {}
+CPU_CHUNK = 128  # shots per task: small, so that the few hard shots do not pin one core
 
 
-def _worker_init(kind, rows, phase_path):
+def _worker_init(kind):
     devnull = os.open(os.devnull, os.O_WRONLY)
     os.dup2(devnull, 1)  # upstream prints one line per shot
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
-    code, errors = workload(0)
+    from library_s_grand_gb300 import workloads
+    w = workloads.prob_bb144()
     _W["lib"] = O.Reference() if kind == "reference" else O.Port()
     _W["O"] = O
-    _W["code"] = code
-    _W["errors"] = errors[rows[0]:rows[1]]
-    _W["phase"] = phase_path
+    _W["w"] = w
+    _W["phase"] = w.phase_file(tempfile.mkdtemp())
 
 
-def _worker_step(_):
-    O = _W["O"]
-    cfg = O.make_config(W_MAX, mode=-1, cap=CAP)
-    t0 = time.perf_counter()
-    r = _W["lib"].css(O.PROB, _W["code"].hx, _W["code"].hz, _W["errors"], None, cfg, "x", _W["phase"])
-    res = r[1]
-    return len(res), int(res["total_tested_combinations"].sum()), time.perf_counter() - t0
+def _worker_chunk(span):
+    """Decode shots [lo, hi) of the headline batch; (shots, candidates tested)."""
+    lo, hi = span
+    O, w = _W["O"], _W["w"]
+    r = _W["lib"].css(O.PROB, w.code.hx, w.code.hz, w.errors[lo:hi], None, O.Config(*w.config),
+                      "x", _W["phase"])
+    assert r[0] == 0
+    return hi - lo, int(r[1]["total_tested_combinations"].sum())
+
+
+def cpu_model() -> str:
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    import platform
+    return platform.processor() or platform.machine()
 
 
 class CpuPool:
-    """One process per host core, each owning a fixed slice of the batch."""
+    """Worker processes fed from one shared task queue of 128-shot chunks.
 
-    def __init__(self, phase_path, cores=None):
+    Passes over the batch are queued together, so while one core works through
+    a pass's few hard shots (one shot of the headline batch tests 8.3e6
+    candidates, 60 % of the pass's work) the others take chunks of the next
+    passes: the figure is a throughput with every core kept busy."""
+
+    def __init__(self, cores=None):
         import multiprocessing as mp
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import oracle as O
         O.build()
         self.kind = "reference" if O.Reference.available() else "port"
         self.cores = cores or os.cpu_count() or 1
-        ctx = mp.get_context("spawn")
-        bounds = np.linspace(0, SHOTS, self.cores + 1).astype(int)
-        self.pools = [ctx.Pool(1, initializer=_worker_init,
-                               initargs=(self.kind, (int(bounds[i]), int(bounds[i + 1])), phase_path))
-                      for i in range(self.cores)]
+        self.pool = mp.get_context("spawn").Pool(self.cores, initializer=_worker_init,
+                                                 initargs=(self.kind,))
+        self.pool.map(_worker_chunk, [(0, 1)] * self.cores, chunksize=1)  # imports, library load
 
-    def step(self):
+    def passes(self, k):
+        """Decode the batch k times; (wall seconds, shots, candidates)."""
+        spans = [(lo, min(lo + CPU_CHUNK, SHOTS)) for _ in range(k)
+                 for lo in range(0, SHOTS, CPU_CHUNK)]
         t0 = time.perf_counter()
-        futs = [p.apply_async(_worker_step, (0,)) for p in self.pools]
-        out = [f.get() for f in futs]
-        return time.perf_counter() - t0, sum(o[0] for o in out), sum(o[1] for o in out)
-
-    def close(self):
-        for p in self.pools:
-            p.terminate()
-
-
-def cpu_baseline(phase_path, seconds=12.0):
-    pool = CpuPool(phase_path)
-    try:
-        pool.step()  # warm-up (imports, library load)
-        t_tot, shots, cands, steps = 0.0, 0, 0, 0
-        while t_tot < seconds and steps < 10000:
-            dt, s, c = pool.step()
-            t_tot += dt
+        shots = cands = 0
+        for s, c in self.pool.imap_unordered(_worker_chunk, spans, chunksize=1):
             shots += s
             cands += c
-            steps += 1
+        return time.perf_counter() - t0, shots, cands
+
+    def close(self):
+        self.pool.terminate()
+        self.pool.join()
+
+
+def cpu_baseline(seconds=12.0):
+    """The upstream CPU algorithm on this host: one core (whole passes) and all cores."""
+    one = CpuPool(cores=1)
+    try:
+        t1, s1, c1 = one.passes(1)
+        passes1 = 1
+        while t1 < 0.25 * seconds and passes1 < 50:
+            dt, s, c = one.passes(1)
+            t1, s1, c1, passes1 = t1 + dt, s1 + s, c1 + c, passes1 + 1
+    finally:
+        one.close()
+    pool = CpuPool()
+    try:
+        pool.passes(1)  # warm-up
+        k = max(2, int(round(0.75 * seconds / max(t1 / passes1, 1e-3) * pool.cores)))
+        k = min(k, 400)
+        t_all, shots, cands = pool.passes(k)
     finally:
         pool.close()
-    return {"value": shots / t_tot, "unit": "shots/s", "cores": pool.cores, "kind": pool.kind,
-            "candidates_per_s": cands / t_tot,
-            "sample": f"{steps} passes over the 16384-shot batch split across {pool.cores} "
-                      f"processes ({t_tot:.1f} s wall), upstream CPU search algorithm, mode -1"}
+    return {"value": shots / t_all, "unit": "shots/s", "cores": pool.cores, "kind": pool.kind,
+            "candidates_per_s": cands / t_all,
+            "value_1core": s1 / t1, "candidates_per_s_1core": c1 / t1,
+            "all_cores_vs_1core": (shots / t_all) / (s1 / t1), "cpu_model": cpu_model(),
+            "sample": f"all cores: {k} passes over the 16384-shot batch as {CPU_CHUNK}-shot tasks "
+                      f"on {pool.cores} processes ({t_all:.1f} s wall); 1 core: {passes1} "
+                      f"pass(es) ({t1:.1f} s); upstream CPU search algorithm, mode -1"}
 
 
 # ---------------------------------------------------------------------------
@@ -207,14 +236,12 @@ def stress_ops(code_h, syndromes, W):
 
 def run_ours(args):
     import torch
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
+    from library_s_grand_gb300 import launch
+    rank, world, local = launch.env_ranks()
+    if world > 1 and world != args.gpus:
+        raise SystemExit(f"bench.py: WORLD_SIZE={world} but --gpus {args.gpus}")
     torch.cuda.set_device(local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    dist = launch.init_from_env("nccl", torch.device("cuda", local))
     from library_s_grand_gb300 import build as B
     from library_s_grand_gb300 import capi, synth
     from library_s_grand_gb300.engine import Engine
@@ -274,12 +301,11 @@ def run_ours(args):
     if eng.sync_status(sp) != 0:
         raise RuntimeError("device decode status error")
     per = np.array([a.elapsed_time(b) for a, b in ev])
-    total_ms = float(per.sum())
-    if dist:
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = launch.max_over_ranks(dist, float(per.sum()), dev)
     value = world * SHOTS * args.steps / (total_ms * 1e-3)
+    if world > 1:
+        sys.stderr.write(f"rank {rank}: n_gpus {world}, {SHOTS * args.steps} shots in "
+                         f"{per.sum():.3f} ms (max over ranks {total_ms:.3f} ms)\n")
 
     # kernel split (non-graph launches with events; median of 5)
     split = []
@@ -352,7 +378,7 @@ def run_ours(args):
             extra["ml_dem"] = bench_ml(torch, lib, dev, sp, flush)
             extra["sampling"] = bench_sampling(torch, lib, dev, sp)
             extra["serving"] = bench_serving(lib)
-        cpu = cpu_baseline(phase, seconds=args.cpu_seconds) if args.cpu_seconds > 0 else None
+        cpu = cpu_baseline(seconds=args.cpu_seconds) if args.cpu_seconds > 0 else None
 
         out = {
             "metric": METRIC, "value": value, "unit": "shots/s", "n_gpus": world,
@@ -735,35 +761,39 @@ def run_case(args):
 
 
 def run_reference(args):
+    """The upstream CPU search algorithm on every host core, on the headline batch: each
+    step is one pass over the 16384 shots; the warm-up passes and then the timed passes
+    are each queued as one set of 128-shot tasks (every core busy)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return None
-    from library_s_grand_gb300 import synth
-    tmp = tempfile.mkdtemp()
-    phase = synth.write_phase_file(os.path.join(tmp, "phase.txt"), PHASE)
-    pool = CpuPool(phase)
+    pool = CpuPool()
     try:
-        for _ in range(args.warmup):
-            pool.step()
-        t_tot, cands = 0.0, 0
-        for _ in range(args.steps):
-            dt, s, c = pool.step()
-            t_tot += dt
-            cands += c
+        if args.warmup:
+            pool.passes(args.warmup)
+        t_tot, shots, cands = pool.passes(args.steps)
     finally:
         pool.close()
-    value = SHOTS * args.steps / t_tot
+    value = shots / t_tot
     return {"metric": METRIC, "value": value, "unit": "shots/s", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_tot * 1e3 / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
             "data": "synthetic (seeded numpy PCG64)", "config": workload_config(),
             "impl": "reference", "candidates_per_s": cands / t_tot,
             "cpu_baseline": {"value": value, "unit": "shots/s", "cores": pool.cores,
-                             "kind": pool.kind,
-                             "sample": f"{args.steps} timed passes over the 16384-shot batch split "
-                                       f"across {pool.cores} processes, mode -1"},
+                             "kind": pool.kind, "cpu_model": cpu_model(),
+                             "sample": f"{args.steps} timed passes over the 16384-shot batch, "
+                                       f"queued together as {CPU_CHUNK}-shot tasks on "
+                                       f"{pool.cores} processes, mode -1"},
             "e2e": {"value": value, "unit": "shots/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
+
+
+def _rank_entry(argd):
+    """One rank of a multi-GPU run started by bench.py itself."""
+    out = run_ours(argparse.Namespace(**argd))
+    if out is not None:
+        print(json.dumps(out), flush=True)
 
 
 def main():
@@ -784,6 +814,18 @@ def main():
     if args.case:
         run_case(args)
         return
+    if args.impl == "ours" and args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        # no outside launcher: one process per GPU, started here (weak scaling: each rank
+        # decodes its own 16384-shot batch)
+        import torch
+        have = torch.cuda.device_count()
+        if have < args.gpus:
+            sys.stderr.write(f"bench.py --gpus {args.gpus}: only {have} CUDA device(s) visible; "
+                             f"a {args.gpus}-rank run needs one GPU per rank\n")
+            sys.exit(2)
+        from library_s_grand_gb300 import launch
+        codes = launch.spawn_ranks(args.gpus, _rank_entry, (vars(args),))
+        sys.exit(0 if all(c == 0 for c in codes) else 1)
     out = run_reference(args) if args.impl == "reference" else run_ours(args)
     if out is not None:
         print(json.dumps(out), flush=True)

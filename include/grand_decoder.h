@@ -158,18 +158,25 @@ int grand_decode_ML_cln_ex(int *H_dem, const int *L_dem, int n, int m, int n_log
  * memory belongs to another framework's pool): it calls no cudaMalloc, cudaFree
  * or other allocating routine.  d_H (n x m int32, the matrix that decodes the
  * syndromes, i.e. Hz for X errors), d_syndromes (num_shots x n int32) and
- * d_results (num_shots records) are device pointers owned by the caller; results
- * equal grand_decode_cc(Hx, Hz, n, m, NULL, syndromes, ...) field for field, with
- * zero timing fields.  Everything else lives in one fixed file-scope device array
- * of about 25 MiB, held by every GPU that loads it until the process exits.
- * Limits: n <= 256, m <= 1024 (larger sizes return GRAND_ERR_LIMIT with a
- * message); hard shots share a 16 MiB search arena per 2048-shot chunk and an
- * exhausted arena also returns GRAND_ERR_LIMIT.  The first call on a device does
- * its set-up (looks up the array's device address, fills its binomial table) and
- * synchronizes `stream`: make it before any stream capture.  Every call reuses
- * the same array, so calls that overlap on the GPU (other threads, other
- * streams) race; the call itself returns only when its work on `stream`
- * (a cudaStream_t, NULL for the legacy default stream) has finished. */
+ * d_results (num_shots records) are device pointers owned by the caller; the
+ * deterministic result fields equal grand_decode_cc(Hx, Hz, n, m, NULL,
+ * syndromes, ...) field for field, and the timing fields are per-shot GPU timer
+ * values as with the other entry points.  Everything else lives in one fixed
+ * file-scope device array of about 25 MiB, held by every GPU that loads it until
+ * the process exits.  Limits: n <= 256, m <= 1024 (larger sizes return
+ * GRAND_ERR_LIMIT with a message).  Shots run in chunks of 2048; hard shots of a
+ * chunk share a 16 MiB search arena, and shots that find it full are re-run in
+ * further rounds of the chunk with the arena emptied; a shot whose search data
+ * alone exceeds the arena gets a zero result and the call returns
+ * GRAND_ERR_LIMIT.  The call reads a status word back after each round, so it
+ * synchronizes `stream` once per chunk.  The first call on a device does its
+ * set-up (looks up the array's device address, fills its binomial table) and
+ * synchronizes `stream`: make it before any stream capture.  Like the other
+ * entry points, it keeps per-device state for the life of the process: after
+ * cudaDeviceReset the process must be restarted before either is called again.
+ * Every call reuses the same array, so calls that overlap on the GPU (other
+ * threads, other streams) race; the call itself returns only when its work on
+ * `stream` (a cudaStream_t, NULL for the legacy default stream) has finished. */
 int grand_decode_cc_noalloc(const int *d_H, int n, int m, const int *d_syndromes, int num_shots,
                             const GrandDecoderConfig *config, GrandDecoderResult *d_results,
                             void *stream);
@@ -200,6 +207,17 @@ int grand_decode_cln_packed(const int *H_dem, const int *L_dem, int n, int m, in
                             const unsigned int *detectors, const unsigned int *logicals,
                             int num_shots, const GrandDecoderConfig *config,
                             GrandDecoderResult *results, int variant, const char *file);
+
+/* Upstream's per-shot stdout line for one result record (no upstream function:
+ * upstream prints it inline, grand_decoder.cu:1230-1238 and :1373-1380 for the CSS
+ * functions with and without supplied errors, :1651-1653 for the DEM functions).
+ * The decoders print these lines with GRAND_VERBOSE=1.  `shot` is the 1-based shot
+ * number printed; returns the line length (as snprintf) or -1 for an unknown kind. */
+#define GRAND_LINE_CSS_SYNDROMES 0
+#define GRAND_LINE_CSS_ERRORS 1
+#define GRAND_LINE_DEM 2
+int grand_format_result(int kind, const GrandDecoderResult *result, int shot, char *buf,
+                        int buf_len);
 
 const char *grand_version(void);
 const char *grand_last_error(void);

@@ -130,34 +130,19 @@ bool verbose() {
 }
 
 void print_css(const GrandDecoderResult *res, int N, bool with_errors) {
+  char line[512];
   for (int i = 0; i < N; ++i) {
-    const GrandDecoderResult *r = &res[i];
-    if (with_errors)
-      printf("shot %d: found=%d, original_weight=%d, found_weight=%d, degenerate=%d, is_equal=%d, "
-             "iteration=%d, tam=%d, total_tested_combinations=%llu, hybrid=%d, time_sum_ms=%.5f, "
-             "total_time_search_ms=%.5f, transfer_time_ms=%.5f, total_to_find_ms=%.5f\n",
-             i + 1, r->found, r->original_weight, r->found_weight, r->degenerate, r->is_equal,
-             r->iteration, r->tam, r->total_tested_combinations, r->hibrido, r->time_sum_ms,
-             r->total_time_search_ms, r->transfer_time_ms, r->total_to_find_ms);
-    else
-      printf("shot %d: found=%d, found_weight=%d, iteration=%d, tam=%d, "
-             "total_tested_combinations=%llu, hybrid=%d, time_sum_ms=%.5f, "
-             "total_time_search_ms=%.5f, transfer_time_ms=%.5f, total_to_find_ms=%.5f\n",
-             i + 1, r->found, r->found_weight, r->iteration, r->tam, r->total_tested_combinations,
-             r->hibrido, r->time_sum_ms, r->total_time_search_ms, r->transfer_time_ms,
-             r->total_to_find_ms);
+    grand_format_result(with_errors ? GRAND_LINE_CSS_ERRORS : GRAND_LINE_CSS_SYNDROMES, &res[i],
+                        i + 1, line, (int)sizeof(line));
+    fputs(line, stdout);
   }
 }
 
 void print_dem(const GrandDecoderResult *res, int N) {
+  char line[512];
   for (int i = 0; i < N; ++i) {
-    const GrandDecoderResult *r = &res[i];
-    printf("shot %d: found=%d, found_weight=%d, degenerate=%d, iteration=%d, tam=%d, "
-           "total_tested_combinations=%llu, hybrid=%d, time_sum_ms=%.5f, total_time_search_ms=%.5f, "
-           "transfer_time_ms=%.5f, total_to_find_ms=%.5f\n",
-           i + 1, r->found, r->found_weight, r->degenerate, r->iteration, r->tam,
-           r->total_tested_combinations, r->hibrido, r->time_sum_ms, r->total_time_search_ms,
-           r->transfer_time_ms, r->total_to_find_ms);
+    grand_format_result(GRAND_LINE_DEM, &res[i], i + 1, line, (int)sizeof(line));
+    fputs(line, stdout);
   }
 }
 
@@ -456,6 +441,38 @@ int grand_decode_cln_packed(const int *H_dem, const int *L_dem, int n, int m, in
   return decode_dem(variant, H_dem, L_dem, n, m, n_logicos, reinterpret_cast<const int *>(detectors),
                     reinterpret_cast<const int *>(logicals), num_shots, config, results, file,
                     nullptr, true);
+}
+
+// Upstream's per-shot stdout line (grand_decoder.cu:1230-1238 / 1373-1380 for the CSS
+// functions with and without supplied errors, :1651-1653 for the DEM functions).
+int grand_format_result(int kind, const GrandDecoderResult *r, int shot, char *buf, int buf_len) {
+  if (!r || !buf || buf_len <= 0) return -1;
+  if (kind == GRAND_LINE_CSS_ERRORS)
+    return snprintf(buf, (size_t)buf_len,
+                    "shot %d: found=%d, original_weight=%d, found_weight=%d, degenerate=%d, "
+                    "is_equal=%d, iteration=%d, tam=%d, total_tested_combinations=%llu, hybrid=%d, "
+                    "time_sum_ms=%.5f, total_time_search_ms=%.5f, transfer_time_ms=%.5f, "
+                    "total_to_find_ms=%.5f\n",
+                    shot, r->found, r->original_weight, r->found_weight, r->degenerate, r->is_equal,
+                    r->iteration, r->tam, r->total_tested_combinations, r->hibrido, r->time_sum_ms,
+                    r->total_time_search_ms, r->transfer_time_ms, r->total_to_find_ms);
+  if (kind == GRAND_LINE_CSS_SYNDROMES)
+    return snprintf(buf, (size_t)buf_len,
+                    "shot %d: found=%d, found_weight=%d, iteration=%d, tam=%d, "
+                    "total_tested_combinations=%llu, hybrid=%d, time_sum_ms=%.5f, "
+                    "total_time_search_ms=%.5f, transfer_time_ms=%.5f, total_to_find_ms=%.5f\n",
+                    shot, r->found, r->found_weight, r->iteration, r->tam,
+                    r->total_tested_combinations, r->hibrido, r->time_sum_ms,
+                    r->total_time_search_ms, r->transfer_time_ms, r->total_to_find_ms);
+  if (kind == GRAND_LINE_DEM)
+    return snprintf(buf, (size_t)buf_len,
+                    "shot %d: found=%d, found_weight=%d, degenerate=%d, iteration=%d, tam=%d, "
+                    "total_tested_combinations=%llu, hybrid=%d, time_sum_ms=%.5f, "
+                    "total_time_search_ms=%.5f, transfer_time_ms=%.5f, total_to_find_ms=%.5f\n",
+                    shot, r->found, r->found_weight, r->degenerate, r->iteration, r->tam,
+                    r->total_tested_combinations, r->hibrido, r->time_sum_ms,
+                    r->total_time_search_ms, r->transfer_time_ms, r->total_to_find_ms);
+  return -1;
 }
 
 const char *grand_version(void) { return "grand-gb300 0.1 (sm_103a)"; }

@@ -38,7 +38,9 @@ constexpr size_t kOffColw = align256(kOffCols + sizeof(uint32_t) * kNaMaxCols * 
 constexpr size_t kOffHcol = align256(kOffColw + sizeof(int) * kNaMaxCols);
 constexpr size_t kOffSmall = align256(kOffHcol + sizeof(uint32_t) * kNaMaxCols);  // counters, +128: status
 constexpr size_t kOffDeferred = align256(kOffSmall + 256);
-constexpr size_t kOffJobs = align256(kOffDeferred + sizeof(int) * kNaChunk);
+constexpr size_t kOffMap = align256(kOffDeferred + sizeof(int) * kNaChunk);     // re-run list
+constexpr size_t kOffMapCount = align256(kOffMap + sizeof(int) * kNaChunk);     // its length
+constexpr size_t kOffJobs = align256(kOffMapCount + 256);
 constexpr size_t kOffArena = align256(kOffJobs + sizeof(Job) * kNaChunk);
 constexpr size_t kScratchBytes = align256(kOffArena + sizeof(uint32_t) * kNaArenaWords);
 
@@ -109,6 +111,30 @@ __global__ void noalloc_code_kernel(DevCode tmpl, const int *colw, int m, DevCod
     tmpl.regular = s_irregular ? 0 : 1;
     *out = tmpl;
   }
+}
+
+// One warp: the ascending list of the chunk's shots that the last round deferred
+// (their heavy-shot staging did not fit the arena), and its length.  Every shot
+// of the chunk had its flag written in the first round, and a re-run rewrites
+// the flags of the shots it runs, so the flags are current for all cnt shots.
+__global__ void noalloc_deferred_kernel(const int *deferred, int cnt, int *map, int *count) {
+  const int lane = threadIdx.x & 31;
+  int base = 0;
+  for (int i0 = 0; i0 < cnt; i0 += 32) {
+    const bool d = i0 + lane < cnt && deferred[i0 + lane] != 0;
+    const unsigned bits = __ballot_sync(0xffffffffu, d);
+    if (d) map[base + __popc(bits & ((1u << lane) - 1u))] = i0 + lane;
+    base += __popc(bits);
+  }
+  if (lane == 0) *count = base;
+}
+
+// Shots that could not be searched within the arena even one at a time: a
+// zero result record (found = 0), so that no stale bytes are left behind.
+__global__ void noalloc_clear_kernel(const int *map, int count, GrandDecoderResult *results) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count * 18) return;
+  reinterpret_cast<uint32_t *>(results + map[i / 18])[i % 18] = 0u;
 }
 
 std::mutex g_mu;
@@ -223,11 +249,18 @@ extern "C" int grand_decode_cc_noalloc(const int *d_H, int n, int m, const int *
   if (e == cudaSuccess) e = cudaMemsetAsync(base + kOffSmall + 128, 0, 128, s);
 
   const Tuning &tn = tuning();
+  // the search kernel's CTAs per SM as the regular entry points choose them
+  const int per_sm = tn.search_grid_mult ? (tn.search_grid_mult < g_sbps[dev] ? tn.search_grid_mult
+                                                                               : g_sbps[dev])
+                                         : g_sbps[dev];
+  int *map = reinterpret_cast<int *>(base + kOffMap);
+  int *map_count = reinterpret_cast<int *>(base + kOffMapCount);
+  unsigned st = 0;       // status bits of every round of every chunk
+  long long unsearched = 0;  // shots whose staging alone exceeds the arena
   for (int lo = 0; lo < num_shots && e == cudaSuccess; lo += kNaChunk) {
     const int cnt = num_shots - lo < kNaChunk ? num_shots - lo : kNaChunk;
     DevBatch b;
     memset(&b, 0, sizeof(b));
-    b.num_shots = cnt;
     b.num_codes = 1;
     b.codes = code;
     b.in = d_syndromes + (size_t)lo * n;
@@ -242,26 +275,53 @@ extern "C" int grand_decode_cc_noalloc(const int *d_H, int n, int m, const int *
     b.deferred = reinterpret_cast<int *>(base + kOffDeferred);
     b.light_max_log2 = tn.light_max_log2;
     b.tile_k = tn.tile_k;
-    // job and tile counters restart for every chunk
-    e = cudaMemsetAsync(base + kOffSmall, 0, 128, s);
-    const int tgrid_max = g_sms[dev] * g_tbps[dev];
-    const int tgrid = (cnt + 3) / 4 < tgrid_max ? (cnt + 3) / 4 : tgrid_max;
-    if (e == cudaSuccess) e = launch_triage(b, tgrid > 0 ? tgrid : 1, s);
-    if (e == cudaSuccess) e = launch_search(b, g_sms[dev] * g_sbps[dev], s);
+    // Rounds: all of the chunk's shots, then, while some heavy shots found the
+    // arena full, only those (their list built on the device), each round with
+    // an empty arena.  A round in which no deferred shot fits means that each of
+    // them alone needs more than the arena: those get a zero result.
+    int todo = cnt;
+    for (int round = 0; e == cudaSuccess; ++round) {
+      b.num_shots = todo;
+      b.shot_map = round == 0 ? nullptr : map;
+      // counters (job, tile, arena, shot) and status restart for every round
+      e = cudaMemsetAsync(base + kOffSmall, 0, 256, s);
+      const int tgrid_max = g_sms[dev] * g_tbps[dev];
+      const int tgrid = (todo + 3) / 4 < tgrid_max ? (todo + 3) / 4 : tgrid_max;
+      if (e == cudaSuccess) e = launch_triage(b, tgrid > 0 ? tgrid : 1, s);
+      if (e == cudaSuccess) e = launch_search(b, g_sms[dev] * per_sm, s);
+      unsigned rs = 0;
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(&rs, base + kOffSmall + 128, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+      if (e != cudaSuccess) break;
+      st |= rs & ~(unsigned)(kStatusScratchOverflow | kStatusJobOverflow);
+      if (!(rs & (kStatusScratchOverflow | kStatusJobOverflow))) break;
+      noalloc_deferred_kernel<<<1, 32, 0, s>>>(b.deferred, cnt, map, map_count);
+      int left = 0;
+      e = cudaGetLastError();
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(&left, map_count, sizeof(int), cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+      if (e != cudaSuccess || left == 0) break;
+      if (left >= todo) {
+        noalloc_clear_kernel<<<(left * 18 + 255) / 256, 256, 0, s>>>(map, left, b.results);
+        e = cudaGetLastError();
+        unsearched += left;
+        break;
+      }
+      todo = left;
+    }
   }
-  unsigned st = 0;
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(&st, base + kOffSmall + 128, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) {
     fprintf(stderr, "grand_decode_cc_noalloc: CUDA error %s\n", cudaGetErrorString(e));
     return GRAND_ERR_CUDA;
   }
-  if (st & (kStatusScratchOverflow | kStatusJobOverflow)) {
+  if (unsearched) {
     fprintf(stderr,
-            "grand_decode_cc_noalloc: the fixed %llu-word search arena filled up; "
-            "results of the affected shots are missing -- decode fewer hard shots per call\n",
-            kNaArenaWords);
+            "grand_decode_cc_noalloc: %lld shot(s) need more than the fixed %llu-word search "
+            "arena on their own; their results are zero (found = 0)\n",
+            unsearched, kNaArenaWords);
     return GRAND_ERR_LIMIT;
   }
   if (st & kStatusTamLimit) {

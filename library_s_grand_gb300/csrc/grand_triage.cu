@@ -761,11 +761,19 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
     unsigned long long off = 0, jslot = 0, tbase = 0, ntl = 0;
     int ok = 1;
     if (lane == 0) {
-      off = atomicAdd(&b.counters[2], words);
-      if (off + words > b.scratch_words) {
-        ok = 0;
-        atomicOr(b.status, kStatusScratchOverflow);
+      // A reservation that does not fit takes nothing, so one oversized shot
+      // does not make the shots after it fail too (they are re-run otherwise).
+      ok = 0;
+      off = *reinterpret_cast<volatile unsigned long long *>(&b.counters[2]);
+      for (int guard = 0; guard < (1 << 16) && off + words <= b.scratch_words; ++guard) {
+        const unsigned long long seen = atomicCAS(&b.counters[2], off, off + words);
+        if (seen == off) {
+          ok = 1;
+          break;
+        }
+        off = seen;
       }
+      if (!ok) atomicOr(b.status, kStatusScratchOverflow);
     }
     ok = __shfl_sync(kFull, ok, 0);
     if (!ok) {

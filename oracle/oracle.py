@@ -49,11 +49,14 @@ def make_config(W, mode=-1, cap=300, thr=10, tpb=256, use_gpu_sum=0) -> Config:
     return Config(W, tpb, use_gpu_sum, cap, thr, mode)
 
 
-def build(quiet: bool = True) -> None:
-    """Compile the port (and the upstream library when its sources exist)."""
+def build(quiet: bool = True, ref_dir: str | None = None) -> None:
+    """Compile the port, and the upstream library when ref_dir (default: the
+    GRAND_REFERENCE_DIR environment variable) holds its sources."""
     out = subprocess.DEVNULL if quiet else None
     subprocess.check_call(["make", "-C", HERE, "port"], stdout=out)
-    subprocess.call(["make", "-C", HERE, "ref"], stdout=out, stderr=out)
+    ref_dir = ref_dir or os.environ.get("GRAND_REFERENCE_DIR")
+    if ref_dir:
+        subprocess.call(["make", "-C", HERE, "ref", f"REF_DIR={ref_dir}"], stdout=out, stderr=out)
 
 
 def _i32(a):

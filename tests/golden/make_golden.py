@@ -10,9 +10,10 @@ Errors/patterns_{72,144}.txt and Syndromes/syndromes_72.txt.  The upstream
 matrices in H_Matrix/ are recorded by SHA-256 of their parsed content, so the
 bivariate-bicycle construction can be checked against them without the files.
 
-Run from the repository root, with the upstream sources at REF_DIR:
+Run from the repository root, with the upstream sources at REF_DIR (the argument,
+or the GRAND_REFERENCE_DIR environment variable):
 
-    python tests/golden/make_golden.py [REF_DIR]
+    python tests/golden/make_golden.py REF_DIR
 """
 from __future__ import annotations
 
@@ -29,6 +30,7 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
 import oracle as O  # noqa: E402
 from library_s_grand_gb300 import synth as S  # noqa: E402
+from library_s_grand_gb300 import workloads as W_  # noqa: E402
 
 OUT = os.path.dirname(os.path.abspath(__file__))
 
@@ -124,7 +126,7 @@ def cpu_branch_only(res):
 
 
 def main(ref_dir):
-    O.build()
+    O.build(ref_dir=ref_dir)
     ref = O.Reference()
     w = Writer(ref)
     mk = O.make_config
@@ -239,6 +241,10 @@ def main(ref_dir):
     # BB[[288]] (5-word columns) random syndromes: exhaustive heavy searches
     rs = (np.random.default_rng(4).random((2, 144)) < 0.5).astype(np.int32)
     w.css("cc_bb288_randsyn_w3", O.UNIFORM, bb288, None, rs, mk(3))
+    # the first shots of the integer-roofline stress input (BB[[144]] random
+    # syndromes, seed 1, W = 4, cap 300): ~1.2e7 candidates each, all tested
+    _, rs = W_.stress_bb144(3, seed=1)
+    w.css("cc_bb144_randsyn_w4", O.UNIFORM, bb144, None, rs, mk(4, cap=300))
 
     with open(os.path.join(OUT, "index.json"), "w", encoding="utf-8") as f:
         json.dump(dict(matrix_sha256=digests, fixtures=w.index), f, indent=1, sort_keys=True)
@@ -246,4 +252,8 @@ def main(ref_dir):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref_dir = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("GRAND_REFERENCE_DIR")
+    if not ref_dir:
+        sys.exit("usage: make_golden.py REF_DIR  (or set GRAND_REFERENCE_DIR): the directory "
+                 "holding the upstream grand_decoder.cu, H_Matrix/, Errors/ and Syndromes/")
+    main(ref_dir)

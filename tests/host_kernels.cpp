@@ -179,6 +179,11 @@ static inline unsigned atomicCAS(unsigned *a, unsigned cmp, unsigned v) {
   __atomic_compare_exchange_n(a, &cmp, v, false, __ATOMIC_SEQ_CST, __ATOMIC_SEQ_CST);
   return cmp;
 }
+static inline unsigned long long atomicCAS(unsigned long long *a, unsigned long long cmp,
+                                           unsigned long long v) {
+  __atomic_compare_exchange_n(a, &cmp, v, false, __ATOMIC_SEQ_CST, __ATOMIC_SEQ_CST);
+  return cmp;
+}
 static std::mutex g_cas_mu;
 static inline void grand_host_cas128(unsigned long long *slot, unsigned long long c0,
                                      unsigned long long c1, unsigned long long n0,

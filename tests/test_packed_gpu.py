@@ -1,7 +1,7 @@
 """Bit-packed record entry points on the GPU: every deterministic result field
-equals the int32 entry points' on the same shots (CSS syndromes and errors,
-uniform and prob; DEM uniform, prob and ML), with junk bits set past the last
-entry of each shot's final word to check that they are ignored."""
+equals the int32 entry points' and the oracle's on the same shots (CSS syndromes
+and errors, uniform and prob; DEM uniform, prob and ML), with junk bits set past
+the last entry of each shot's final word to check that they are ignored."""
 import numpy as np
 import pytest
 
@@ -21,7 +21,7 @@ def _junk(words, n):
 
 @pytest.mark.parametrize("records", ["syndromes", "errors"])
 @pytest.mark.parametrize("prob", [False, True])
-def test_css_packed_equals_int32(gpulib, tmp_path, records, prob):
+def test_css_packed_equals_int32_and_oracle(gpulib, port, tmp_path, records, prob):
     code = synth.BB_CODES[72]()
     errors, syndromes = synth.css_shots(code.hz, 700, 0.03, seed=41)
     pf = synth.write_phase_file(str(tmp_path / "p.txt"), [(300, 0, 1, 2, 1, 0, 0)]) if prob else None
@@ -39,11 +39,17 @@ def test_css_packed_equals_int32(gpulib, tmp_path, records, prob):
     rc, res = capi.decode_css_packed(gpulib, code.hx, code.hz, words, kind, cfg, "x", pf)
     assert rc == 0
     assert len(O.fields_equal(res, ref)) == 0
+    prc, pres, _ = port.css(O.PROB if prob else O.UNIFORM, code.hx, code.hz,
+                            errors if records == "errors" else None,
+                            syndromes if records == "syndromes" else None,
+                            O.Config(*[getattr(cfg, f) for f, _ in cfg._fields_]), "x", pf)
+    assert prc == 0
+    assert len(O.fields_equal(res, pres)) == 0
     assert res["found"].sum() > 100
 
 
 @pytest.mark.parametrize("variant", ["uniform", "prob", "ml"])
-def test_dem_packed_equals_int32(gpulib, tmp_path, variant):
+def test_dem_packed_equals_int32_and_oracle(gpulib, port, tmp_path, variant):
     dem = synth.random_dem(7, detectors=70, mechanisms=260, logicals=5, p_range=(2e-3, 2e-2))
     det, log, _ = synth.dem_shots(dem, 700, seed=43)
     f = None
@@ -59,5 +65,10 @@ def test_dem_packed_equals_int32(gpulib, tmp_path, variant):
                                      _junk(capi.pack_bits(log), dem.n_logicos), cfg, f)
     assert rc == 0
     assert len(O.fields_equal(res, ref)) == 0
+    v = {"uniform": O.UNIFORM, "prob": O.PROB, "ml": O.ML}[variant]
+    prc, pres, *_ = port.dem(v, dem.h, dem.l, det, log,
+                             O.Config(*[getattr(cfg, f) for f, _ in cfg._fields_]), f)
+    assert prc == 0
+    assert len(O.fields_equal(res, pres)) == 0
     assert res["found"].sum() > 100
 

@@ -2,7 +2,7 @@
 serving mix (four bivariate-bicycle codes with syndrome records, W = 3, and the
 120 x 720 random DEM in ML mode) are submitted concurrently from several threads
 and replayed as a Poisson trace; every request's results must equal those of
-decoding that request alone."""
+decoding that request alone and the oracle's for each of its shots."""
 import threading
 
 import numpy as np
@@ -29,7 +29,7 @@ def serving(gpulib, tmp_path_factory):
         codes.append(("css", c))
     eng.add_dem(dem.h, dem.l, capi.GrandDecoderConfig(3, 256, 0, 64, 10, -1), 2, lf)
     codes.append(("dem", dem))
-    return eng, codes
+    return eng, codes, lf
 
 
 def make_requests(codes, count, seed):
@@ -51,6 +51,28 @@ def make_requests(codes, count, seed):
     return reqs
 
 
+def by_oracle(codes, cid, rec, lf):
+    """Each shot decoded by the oracle (shots of one code decoded together, in order)."""
+    port = O.Port()
+    lens = np.array([codes[c][1].n + (codes[c][1].n_logicos if codes[c][0] == "dem" else 0)
+                     for c in range(len(codes))])
+    starts = np.concatenate([[0], np.cumsum(lens[cid])[:-1]])
+    out = np.zeros(len(cid), dtype=O.RESULT_DTYPE)
+    cfg = O.make_config(3, cap=64)
+    for c, (kind, code) in enumerate(codes):
+        idx = np.nonzero(cid == c)[0]
+        if len(idx) == 0:
+            continue
+        rows = np.stack([rec[starts[i]:starts[i] + lens[c]] for i in idx])
+        if kind == "css":
+            rc, r, _ = port.css(O.UNIFORM, code.hx, code.hz, None, rows, cfg, "x")
+        else:
+            rc, r, *_ = port.dem(O.ML, code.h, code.l, rows[:, :code.n], rows[:, code.n:], cfg, lf)
+        assert rc == 0
+        out[idx] = r
+    return out
+
+
 def alone(eng, req):
     cid, rec = req
     rc, res = eng.decode(rec, cid)
@@ -58,8 +80,8 @@ def alone(eng, req):
     return res
 
 
-def test_concurrent_requests_equal_alone(serving):
-    eng, codes = serving
+def test_concurrent_requests_equal_alone_and_oracle(serving):
+    eng, codes, lf = serving
     srv = Server(eng, slots=3, max_shots_per_batch=1024)
     slots, nbytes = srv.info()
     assert slots == 3 and nbytes > 0
@@ -83,11 +105,12 @@ def test_concurrent_requests_equal_alone(serving):
         t.join()
     for i, req in enumerate(reqs):
         assert len(O.fields_equal(got[i], alone(eng, req))) == 0, i
+        assert len(O.fields_equal(got[i], by_oracle(codes, *req, lf))) == 0, i
     srv.close()
 
 
-def test_poisson_replay_equals_alone(serving):
-    eng, codes = serving
+def test_poisson_replay_equals_alone_and_oracle(serving):
+    eng, codes, lf = serving
     srv = Server(eng, slots=4, max_shots_per_batch=2048)
     reqs = make_requests(codes, 200, 2)
     rng = np.random.default_rng(3)
@@ -101,11 +124,12 @@ def test_poisson_replay_equals_alone(serving):
     rc2, ref = eng.decode(rec, sc)
     assert rc2 == 0
     assert len(O.fields_equal(res, ref)) == 0
+    assert len(O.fields_equal(res, by_oracle(codes, sc, rec, lf))) == 0
     srv.close()
 
 
 def test_admission_by_memory(serving):
-    eng, _ = serving
+    eng, _, _ = serving
     srv = Server(eng, slots=8, max_shots_per_batch=1024, hbm_budget_bytes=2 * 45 * (1 << 20))
     slots, nbytes = srv.info()
     assert 1 <= slots < 8 and nbytes <= 2 * 45 * (1 << 20)
