@@ -9,10 +9,11 @@ synthetic data (numpy PCG64); no dataset exists for this workload.
 
 Reported (one JSON line, rank 0):
   value      shots/s of the persistent batched decoder, records resident in HBM,
-             graph-replayed triage + search launches, L2 flushed between steps;
+             graph-replayed decode launches (one persistent kernel per batch), L2
+             flushed between steps;
   e2e        shots/s through the upstream-compatible C ABI (grand_decode_prob_cc)
              from host buffers, copies included;
-  roofline   the search kernel on the stress input the integer roofline is
+  roofline   the decode kernel on the stress input the integer roofline is
              defined on (random syndromes, W = 4, exhaustive enumeration), ops
              counted as ceil(R/32)+1 per candidate (the fixed (w+1)*ceil(R/32)
              count is reported beside it), against the measured lop3 issue rate;
@@ -314,8 +315,8 @@ def run_ours(args):
         eng.decode_device(SHOTS, d_rec.data_ptr(), d_res.data_ptr(), sp, use_graph=False)
         eng.sync_status(sp)
         split.append(eng.kernel_times(sp))
-    tri_ms, sea_ms = (float(np.median([x[i] for x in split])) for i in range(2))
-    hbm = hbm_streaming(code, tri_ms)
+    reset_ms, dec_ms = (float(np.median([x[i] for x in split])) for i in range(2))
+    hbm = hbm_streaming(code, dec_ms)
 
     out = None
     if rank == 0:
@@ -390,12 +391,12 @@ def run_ours(args):
             "latency_ms": {"p50": float(np.percentile(per, 50)), "p99": float(np.percentile(per, 99)),
                            "what": "per 16384-shot batch, device-resident, graph replay"},
             "plain_shots_per_s": n_plain / plain_s,
-            "plain_what": "one call per shot: H2D record, triage+search launches, sync, D2H",
+            "plain_what": "one call per shot: H2D record, decode launch, sync, D2H",
             "persistent_vs_plain": value / world / (n_plain / plain_s),
-            "kernel_ms": {"triage": tri_ms, "search": sea_ms},
+            "kernel_ms": {"decode": dec_ms, "control_reset": reset_ms},
             "e2e": e2e, "e2e_packed": e2e_packed, "roofline": roof, "hbm_streaming": hbm,
             "cpu_baseline": cpu, "clocks": clk,
-            "gpu_launches": 2 * args.steps,
+            "gpu_launches": args.steps,
         }
         out.update(extra)
     if dist:
@@ -419,16 +420,16 @@ def hbm_peak():
         return 6800.0, "fallback"
 
 
-def hbm_streaming(code, tri_ms):
-    """Record streaming of the triage kernel on the headline batch: int32 error records in
+def hbm_streaming(code, dec_ms):
+    """Record streaming of the decode kernel on the headline batch: int32 error records in
     (4m bytes per shot) and 72-byte results out, per launch, over the kernel's event time."""
     peak, src = hbm_peak()
     per_shot = 4 * code.m + 72
-    gbs = SHOTS * per_shot / (tri_ms * 1e-3) / 1e9
-    return {"kernel": "triage_kernel", "achieved": gbs, "peak": peak, "unit": "GB/s",
+    gbs = SHOTS * per_shot / (dec_ms * 1e-3) / 1e9
+    return {"kernel": "decode_kernel", "achieved": gbs, "peak": peak, "unit": "GB/s",
             "frac": gbs / peak, "peak_source": src + " copy bandwidth (MEASURED_PEAKS.json)",
             "algorithmic_bytes_per_launch": SHOTS * per_shot, "traffic": TRIAGE_TRAFFIC,
-            "traffic_unit": "bytes per launch (ncu)", "triage_ms": tri_ms,
+            "traffic_unit": "bytes per launch (ncu)", "decode_ms": dec_ms,
             "what": "bytes per launch: int32 error records (4m per shot) + 72-byte results"}
 
 
@@ -483,7 +484,7 @@ def stress_roofline(torch, lib, dev, sp):
     return {"bound": "int_alu", "achieved": achieved / 1e9, "peak": peak / 1e9, "unit": "Gop/s",
             "frac": achieved / peak, "traffic": STRESS_TRAFFIC_PER_SHOT * n,
             "traffic_unit": "bytes per launch (ncu, scaled from 48 shots)",
-            "kernel": "search_kernel",
+            "kernel": "decode_kernel",
             "workload": f"{n} random-syndrome shots of BB[[144,12,12]], W=4, exhaustive "
                         f"({cands} candidates, 3 threshold iterations)",
             "ops_per_candidate": "1.5 (sketch XOR + half a 3-way min)",
@@ -756,8 +757,8 @@ def run_case(args):
             raise RuntimeError("decode failed")
         if eng.sync_status(sp) != 0:
             raise RuntimeError("status error")
-        tri, sea = eng.kernel_times(sp)
-        print(f"case {args.case}: triage {tri:.4f} ms  search {sea:.4f} ms", flush=True)
+        rst, dec = eng.kernel_times(sp)
+        print(f"case {args.case}: decode kernel {dec:.4f} ms (control reset {rst:.4f} ms)", flush=True)
 
 
 def run_reference(args):

@@ -4,9 +4,9 @@
  * No upstream counterpart: upstream decodes one code per call with a serial
  * host loop over shots (grand_decoder.cu:885, 1199, 1466, 1762, 2073).  An
  * engine keeps any number of registered codes resident on the GPU and decodes
- * batches whose shots may use different codes, in one triage launch plus one
- * persistent work-stealing search launch, optionally replayed from a captured
- * CUDA graph.  Results are identical to the five grand_decode_* calls on the
+ * batches whose shots may use different codes in one persistent launch (its
+ * warps classify shots, triage the hard ones and search the heaviest, work
+ * stealing from each other), optionally replayed from a captured CUDA graph.  Results are identical to the five grand_decode_* calls on the
  * same shots.
  *
  * Shot records are int32 0/1 rows: the syndrome (n entries) or the error (m
@@ -85,38 +85,40 @@ int grand_engine_decode_device(GrandEngine *engine, int num_shots, const int *d_
 int grand_engine_sync_status(GrandEngine *engine, void *stream);
 
 /* The reference-style one-launch-per-call path: every shot is its own call
- * (host-to-device copy of its record, its triage and search launches, a
- * synchronous read-back of its result), as upstream's GPU mode does per shot.
+ * (host-to-device copy of its record, its decoding launch, a synchronous
+ * read-back of its result), as upstream's GPU mode does per shot.
  * Kept for comparison with the batched path. */
 int grand_engine_decode_plain(GrandEngine *engine, int num_shots, const int *shot_code,
                               const int *records, GrandDecoderResult *results);
 
 /* Tuning knobs (also set by the GRAND_* environment variables):
- * light_log2: largest per-shot search (2^x candidates) finished inside the
- * triage warp; tile_k: prefixes per lane per search tile; search_ctas_per_sm:
- * resident CTAs of the persistent search kernel (0 = occupancy maximum). */
+ * light_log2: largest per-shot search (2^x candidates) finished by the warp
+ * that triages the shot (larger ones become Jobs that every warp searches);
+ * tile_k: prefixes per lane per search tile; search_ctas_per_sm: resident CTAs
+ * per SM of the persistent decode kernel (0 = occupancy maximum). */
 int grand_engine_set_tuning(GrandEngine *engine, int light_log2, int tile_k,
                             int search_ctas_per_sm);
 
-/* Device times of the triage and search kernels of the last non-graph device
- * decode on `stream` (valid after grand_engine_sync_status). */
-int grand_engine_kernel_times(GrandEngine *engine, void *stream, float *triage_ms,
-                              float *search_ms);
+/* Device times of the last non-graph device decode on `stream` (valid after
+ * grand_engine_sync_status): *reset_ms the control-word reset before the
+ * launch, *decode_ms the decode kernel. */
+int grand_engine_kernel_times(GrandEngine *engine, void *stream, float *reset_ms,
+                              float *decode_ms);
 
 /* Times of the last host-buffer decode (grand_engine_decode / _decode_plain):
- * copies in, the triage kernel(s), the search kernel(s) and copies out, from
- * CUDA events on the call's stream.  With zero-copy (records read and results
+ * copies in, the control-word reset(s), the decode kernel(s) and copies out,
+ * from CUDA events on the call's stream.  With zero-copy (records read and results
  * written in place over NVLink-C2C) the copy times are ~0 and the kernels'
  * times include reading host memory.  Any pointer may be NULL. */
-int grand_engine_batch_times(GrandEngine *engine, float *h2d_ms, float *triage_ms,
-                             float *search_ms, float *d2h_ms);
+int grand_engine_batch_times(GrandEngine *engine, float *h2d_ms, float *reset_ms,
+                             float *decode_ms, float *d2h_ms);
 
 /* Diagnostic: sustained 32-bit logic-op (lop3) issue rate of the current device
- * in ops/s, the ceiling of the search kernel's integer roofline; < 0 on error. */
+ * in ops/s, the ceiling of the search's integer roofline; < 0 on error. */
 double grand_measure_int_peak(void);
 
 /* Diagnostic: one line describing the current device as the library sees it
- * (SM count, resident CTAs per SM of both kernels, whether the GPU can read
+ * (SM count, resident CTAs per SM of the decode kernel, whether the GPU can read
  * pageable host memory directly).  Returns the length written or < 0. */
 int grand_device_info(char *buf, int len);
 

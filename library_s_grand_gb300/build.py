@@ -22,8 +22,9 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgranddecoder.so")
 
-SOURCES = ["grand_triage.cu", "grand_search.cu", "grand_peak.cu", "grand_host.cpp", "grand_capi.cpp",
-           "grand_engine.cpp", "grand_noalloc.cu", "grand_server.cpp", "grand_sample.cu"]
+SOURCES = ["grand_decode_plain.cu", "grand_decode_ml.cu", "grand_peak.cu", "grand_host.cpp",
+           "grand_capi.cpp", "grand_engine.cpp", "grand_noalloc.cu", "grand_server.cpp",
+           "grand_sample.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", CSRC, "-I", INCLUDE]
 

@@ -63,6 +63,21 @@ enum StatusBits : unsigned {
   kStatusJobOverflow = 1u << 1,   // heavy-job table full: shot deferred
   kStatusScratchOverflow = 1u << 2,
   kStatusCasLimit = 1u << 3,      // bounded CAS loop gave up (never expected)
+  kStatusWaitLimit = 1u << 4,     // a bounded wait for another warp gave up (never expected)
+};
+
+// Batch control words (DevBatch::counters, 32 x u64, zeroed before every launch).
+enum Counter {
+  kCtrJobsReserved = 0,   // (jobs << 40) | tiles, reserved by publishing warps
+  kCtrNextTile = 1,       // next search tile to draw
+  kCtrScratchTop = 2,     // words of the scratch arena in use
+  kCtrNextChunk = 3,      // next 32-slot classification chunk to draw
+  kCtrQueuePublished = 4, // slow-queue entries readable (published in reservation order)
+  kCtrQueueHead = 5,      // slow-queue entries drawn
+  kCtrChunksDone = 6,     // classification chunks finished
+  kCtrSlowDone = 7,       // slow-path shots finished (their Jobs published)
+  kCtrJobsPublished = 8,  // (jobs << 40) | tiles whose Jobs are fully written
+  kCtrQueueReserved = 9,  // slow-queue entries reserved by appending warps
 };
 
 // Immutable per-code tables plus the per-call search parameters.
@@ -89,6 +104,9 @@ struct DevCode {
   const uint32_t *lcols;     // m * nlw
   const float *llr;          // m
   const uint32_t *hcol;      // m column sketches
+  int binary;                // every entry of H is 0 or 1 (column weights are popcounts)
+  const int *lowstart;       // R + 1: columns grouped by their lowest set row r are
+  const int *lowcols;        //   lowcols[lowstart[r] .. lowstart[r+1]) (nullptr: no groups)
 };
 
 // One searched weight block of one threshold iteration.
@@ -124,10 +142,13 @@ struct IterInfo {
   float *llr;                // tam LLRs in the same order (ML)
 };
 
-// A shot whose search space is too large for one warp: searched by every
-// warp of the persistent search kernel, tile by tile.  16-byte aligned: the
-// ML minima are updated with 128-bit compare-and-swap.
-struct alignas(16) Job {
+// A shot whose search space is too large for one warp: searched by every warp
+// of the launch, tile by tile.  Aligned to (and a multiple of) 128 bytes, so no
+// cache line holds parts of two Jobs: a Job is written once before it is
+// published, and a line another SM cached from a published Job never carries
+// bytes of a Job published later.  (The ML minima, updated with 128-bit
+// compare-and-swap, need 16-byte alignment.)
+struct alignas(128) Job {
   int shot, code;
   int n_it;
   int nseg;
@@ -148,7 +169,7 @@ struct alignas(16) Job {
   Seg seg[kMaxSegs];
   alignas(16) unsigned long long mlkey[kMaxIters][kMaxW + 1][2]; // ML: {cost key, lex rank} minima
 };
-static_assert(sizeof(Job) % 16 == 0, "Job must keep 16-byte alignment in arrays");
+static_assert(sizeof(Job) % 128 == 0, "Job must fill whole 128-byte lines in arrays");
 
 // Everything one batched launch needs.
 struct DevBatch {
@@ -168,12 +189,14 @@ struct DevBatch {
   const unsigned long long *ncr; // (kMaxTam + 1) x (kMaxW + 1)
   Job *jobs;
   int max_jobs;
-  unsigned long long *counters;  // [0] packed job/tile append, [1] next tile, [2] scratch top,
-                                 // [3] next shot slot (triage)
+  unsigned long long *counters;  // control words (enum Counter)
   uint32_t *scratch;
   unsigned long long scratch_words;
   unsigned *status;
   int *deferred;                 // per shot: 1 if the shot must be re-run
+  int *queue;                    // num_shots slots: launch slots that need the per-shot path
+  int fast;                      // 1: settle shots 32 at a time first (empty syndromes, and
+                                 //    weight-1 matches of a one-position first iteration)
   int light_max_log2;            // light-path budget (candidates, log2)
   int tile_k;                    // prefixes per lane per colex tile (weights <= 2)
   int has_ml;                    // some code of the batch is ML: launch the kernels' ML builds

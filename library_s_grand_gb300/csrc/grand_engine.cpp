@@ -241,7 +241,8 @@ int grand_engine_decode_device(GrandEngine *e, int num_shots, const int *d_shot_
   cudaError_t r = ensure(&slot->d_jobs, &slot->cap_jobs, sizeof(Job) * (size_t)max_jobs);
   if (r == cudaSuccess) r = ensure(&slot->d_scratch, &slot->cap_scratch, scratch_words * 4);
   if (r == cudaSuccess) r = ensure(&slot->d_small, &slot->cap_small, 256);
-  if (r == cudaSuccess) r = ensure(&slot->d_deferred, &slot->cap_deferred, sizeof(int) * num_shots);
+  if (r == cudaSuccess)
+    r = ensure(&slot->d_deferred, &slot->cap_deferred, 2 * sizeof(int) * (size_t)num_shots);
   if (r != cudaSuccess) {
     set_error("grand: device workspace allocation failed (%s)", cudaGetErrorString(r));
     return GRAND_ERR_CUDA;
@@ -263,6 +264,8 @@ int grand_engine_decode_device(GrandEngine *e, int num_shots, const int *d_shot_
   b.scratch = (uint32_t *)slot->d_scratch;
   b.scratch_words = scratch_words;
   b.deferred = (int *)slot->d_deferred;
+  b.queue = (int *)slot->d_deferred + num_shots;
+  b.fast = e->tn.fast;
   b.light_max_log2 = e->tn.light_max_log2;
   b.tile_k = e->tn.tile_k;
   for (const DevCode &c : e->codes) b.has_ml |= c.variant == kMl;
@@ -331,18 +334,18 @@ int grand_engine_sync_status(GrandEngine *e, void *stream) {
   return 0;
 }
 
-int grand_engine_batch_times(GrandEngine *e, float *h2d_ms, float *triage_ms, float *search_ms,
+int grand_engine_batch_times(GrandEngine *e, float *h2d_ms, float *reset_ms, float *decode_ms,
                              float *d2h_ms) {
   if (!e) return GRAND_ERR_INVALID;
   std::lock_guard<std::mutex> lk(e->mu);
   if (h2d_ms) *h2d_ms = e->last.h2d_ms;
-  if (triage_ms) *triage_ms = e->last.triage_ms;
-  if (search_ms) *search_ms = e->last.search_ms;
+  if (reset_ms) *reset_ms = e->last.reset_ms;
+  if (decode_ms) *decode_ms = e->last.decode_ms;
   if (d2h_ms) *d2h_ms = e->last.d2h_ms;
   return 0;
 }
 
-int grand_engine_kernel_times(GrandEngine *e, void *stream, float *triage_ms, float *search_ms) {
+int grand_engine_kernel_times(GrandEngine *e, void *stream, float *reset_ms, float *decode_ms) {
   if (!e) return GRAND_ERR_INVALID;
   std::lock_guard<std::mutex> lk(e->mu);
   auto it = e->slots.find(stream);
@@ -351,8 +354,8 @@ int grand_engine_kernel_times(GrandEngine *e, void *stream, float *triage_ms, fl
   if (cudaEventElapsedTime(&a, it->second->ev[0], it->second->ev[1]) != cudaSuccess ||
       cudaEventElapsedTime(&b, it->second->ev[1], it->second->ev[2]) != cudaSuccess)
     return GRAND_ERR_CUDA;
-  if (triage_ms) *triage_ms = a;
-  if (search_ms) *search_ms = b;
+  if (reset_ms) *reset_ms = a;
+  if (decode_ms) *decode_ms = b;
   return 0;
 }
 
@@ -362,9 +365,8 @@ int grand_device_info(char *buf, int len) {
   if (!ctx) return err;
   if (!buf || len <= 0) return GRAND_ERR_INVALID;
   return snprintf(buf, (size_t)len,
-                  "device=%d sms=%d triage_ctas_per_sm=%d search_ctas_per_sm=%d "
-                  "pageable_memory_access=%d",
-                  ctx->device, ctx->sm_count, ctx->triage_bps, ctx->search_bps,
+                  "device=%d sms=%d decode_ctas_per_sm=%d pageable_memory_access=%d",
+                  ctx->device, ctx->sm_count, ctx->decode_bps,
                   ctx->pageable_access);
 }
 

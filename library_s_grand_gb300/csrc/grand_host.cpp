@@ -39,6 +39,7 @@ Tuning &tuning() {
     if (const char *s = getenv("GRAND_TILE_K")) x.tile_k = std::max(1, std::min(64, atoi(s)));
     if (const char *s = getenv("GRAND_SEARCH_GRID_MULT")) x.search_grid_mult = std::max(0, atoi(s));
     if (const char *s = getenv("GRAND_ZERO_COPY")) x.zero_copy = atoi(s) != 0;
+    if (const char *s = getenv("GRAND_FAST")) x.fast = atoi(s) != 0;
     return x;
   }();
   return t;
@@ -64,6 +65,8 @@ CodeTables::~CodeTables() {
   cudaFree(pivrow);
   cudaFree(lcols);
   cudaFree(hcol);
+  cudaFree(lowstart);
+  cudaFree(lowcols);
 }
 
 Workspace::~Workspace() {
@@ -127,10 +130,7 @@ Context *Context::get(int *err) {
   int pa = 0;
   cudaDeviceGetAttribute(&pa, cudaDevAttrPageableMemoryAccess, dev);
   c->pageable_access = pa;
-  if (occupancy(&c->triage_bps, &c->search_bps) != cudaSuccess) {
-    c->triage_bps = 4;
-    c->search_bps = 2;
-  }
+  if (decode_occupancy(&c->decode_bps) != cudaSuccess || c->decode_bps < 1) c->decode_bps = 1;
   std::vector<unsigned long long> t((size_t)(kMaxTam + 1) * (kMaxW + 1));
   for (int n = 0; n <= kMaxTam; ++n)
     for (int k = 0; k <= kMaxW; ++k) t[(size_t)n * (kMaxW + 1) + k] = ncr_host(n, k);
@@ -266,14 +266,35 @@ std::shared_ptr<CodeTables> Context::tables(int family, const int *H, const int 
   for (int c = 1; c < m; ++c)
     if (colw[c] != colw[0]) { t->regular = 0; break; }
   std::vector<uint32_t> hcol(m, 0u);
+  t->binary = 1;
+  std::vector<int> lowrow(m, -1);  // lowest set row of each column
   for (int r = 0; r < n; ++r) {
     const uint32_t hr = row_hash(r);
+    for (int c = 0; c < m; ++c) {
+      const int v = H[(size_t)r * m + c];
+      if (v != 0) {
+        hcol[c] ^= hr;
+        if (lowrow[c] < 0) lowrow[c] = r;
+      }
+      if (v != 0 && v != 1) t->binary = 0;
+    }
+  }
+  // nonzero columns grouped by their lowest row (ascending within a group)
+  std::vector<int> lowstart(n + 1, 0), lowcols;
+  for (int c = 0; c < m; ++c)
+    if (lowrow[c] >= 0) ++lowstart[lowrow[c] + 1];
+  for (int r = 0; r < n; ++r) lowstart[r + 1] += lowstart[r];
+  lowcols.assign(lowstart[n], 0);
+  {
+    std::vector<int> fill(lowstart.begin(), lowstart.end() - 1);
     for (int c = 0; c < m; ++c)
-      if (H[(size_t)r * m + c] != 0) hcol[c] ^= hr;
+      if (lowrow[c] >= 0) lowcols[fill[lowrow[c]]++] = c;
   }
   cudaError_t e = upload(&t->cols, cols);
   if (e == cudaSuccess) e = upload(&t->colw, colw);
   if (e == cudaSuccess) e = upload(&t->hcol, hcol);
+  if (e == cudaSuccess) e = upload(&t->lowstart, lowstart);
+  if (e == cudaSuccess) e = upload(&t->lowcols, lowcols);
   if (e == cudaSuccess && family == kCss) {
     std::vector<uint32_t> rows((size_t)n * t->mw, 0u);
     for (int r = 0; r < n; ++r)
@@ -346,21 +367,26 @@ DevCode make_devcode(const CodeTables &t, const CallParams &p) {
   d.lcols = t.lcols;
   d.llr = p.d_llr;
   d.hcol = t.hcol;
+  d.binary = t.binary;
+  d.lowstart = t.lowstart;
+  d.lowcols = t.lowcols;
   return d;
+}
+
+int decode_blocks_per_sm(int occupancy_bps, const Tuning &tn) {
+  const int occ = std::max(occupancy_bps, 1);
+  return tn.search_grid_mult ? std::min(tn.search_grid_mult, occ) : occ;
 }
 
 cudaError_t launch_pipeline(const Context *ctx, const DevBatch &b, const Tuning &tn,
                             cudaStream_t s, cudaEvent_t mid) {
   cudaError_t e = cudaMemsetAsync(b.counters, 0, 256, s);
   if (e != cudaSuccess) return e;
-  const int tgrid_max = ctx->sm_count * std::max(ctx->triage_bps, 1);
-  const int tgrid = std::max(1, std::min(tgrid_max, (b.num_shots + 3) / 4));
-  e = launch_triage(b, tgrid, s);
-  if (e != cudaSuccess) return e;
   if (mid) cudaEventRecord(mid, s);
-  const int per_sm = tn.search_grid_mult ? std::min(tn.search_grid_mult, std::max(ctx->search_bps, 1))
-                                         : std::max(ctx->search_bps, 1);
-  return launch_search(b, ctx->sm_count * per_sm, s);
+  // persistent: as many blocks as are resident at once (fewer for a small batch,
+  // whose shots and tiles would leave most warps idle)
+  const int full = ctx->sm_count * decode_blocks_per_sm(ctx->decode_bps, tn);
+  return launch_decode(b, full, s);
 }
 
 int run_batch(Context *ctx, Workspace *ws, const BatchRequest &req, BatchTiming *timing,
@@ -390,7 +416,7 @@ int run_batch(Context *ctx, Workspace *ws, const BatchRequest &req, BatchTiming 
   CK(ensure(&ws->d_scratch, &ws->cap_scratch, scratch_words * 4));
   size_t small_cap = ws->d_small ? 256 : 0;
   CK(ensure(&ws->d_small, &small_cap, 256));
-  CK(ensure(&ws->d_deferred, &ws->cap_deferred, sizeof(int) * N));
+  CK(ensure(&ws->d_deferred, &ws->cap_deferred, 2 * sizeof(int) * N));
 
   // Per-call host work is kept to the launches, one status read and one
   // synchronisation; events are recorded only when the caller asks for times,
@@ -461,6 +487,8 @@ int run_batch(Context *ctx, Workspace *ws, const BatchRequest &req, BatchTiming 
   b.scratch = (uint32_t *)ws->d_scratch;
   b.scratch_words = scratch_words;
   b.deferred = (int *)ws->d_deferred;
+  b.queue = (int *)ws->d_deferred + N;
+  b.fast = tn.fast;
   b.light_max_log2 = tn.light_max_log2;
   b.tile_k = tn.tile_k;
   for (const DevCode &c : req.codes) b.has_ml |= c.variant == kMl;
@@ -524,8 +552,8 @@ int run_batch(Context *ctx, Workspace *ws, const BatchRequest &req, BatchTiming 
     cudaEventElapsedTime(&h2d, ws->ev[0], ws->ev[1]);
     cudaEventElapsedTime(&d2h, ws->ev[4], ws->ev[5]);
     timing->h2d_ms = h2d;
-    timing->triage_ms = tri_ms;
-    timing->search_ms = sea_ms;
+    timing->reset_ms = tri_ms;
+    timing->decode_ms = sea_ms;
     timing->d2h_ms = d2h;
     timing->rounds = rounds;
   }

@@ -12,14 +12,12 @@
 
 namespace grand {
 
-// Kernel launchers (grand_triage.cu, grand_search.cu).
-cudaError_t launch_triage(const DevBatch &b, int grid, cudaStream_t s);
-cudaError_t launch_search(const DevBatch &b, int grid, cudaStream_t s);
-cudaError_t triage_occupancy(int *blocks_per_sm);
+// Kernel launchers (grand_decode_plain.cu, grand_decode_ml.cu, grand_sample.cu).
+cudaError_t launch_decode(const DevBatch &b, int grid, cudaStream_t s);
+cudaError_t decode_occupancy(int *blocks_per_sm);
 cudaError_t launch_sample(const DevCode &cd, const float *d_p, unsigned long long seed,
                           unsigned long long first_shot, int num_shots, int *d_records,
-                          int sm_count, cudaStream_t s);  // grand_sample.cu
-cudaError_t occupancy(int *triage_blocks_per_sm, int *search_blocks_per_sm);
+                          int sm_count, cudaStream_t s);
 
 void set_error(const char *fmt, ...);
 
@@ -36,6 +34,9 @@ struct CodeTables {
   int *pivrow = nullptr;
   uint32_t *lcols = nullptr;
   uint32_t *hcol = nullptr;  // column sketches (row_hash XOR over each column's rows)
+  int binary = 1;             // every entry is 0 or 1
+  int *lowstart = nullptr;    // R + 1: nonzero columns grouped by their lowest row
+  int *lowcols = nullptr;
   std::vector<int> key;  // exact content the tables were built from
   size_t bytes = 0;
   ~CodeTables();
@@ -70,7 +71,7 @@ struct Workspace {
   void *d_jobs = nullptr; size_t cap_jobs = 0;
   void *d_scratch = nullptr; size_t cap_scratch = 0;
   void *d_small = nullptr;  // counters, status
-  void *d_deferred = nullptr; size_t cap_deferred = 0;
+  void *d_deferred = nullptr; size_t cap_deferred = 0;  // 2 x shots: flags, then the slow queue
   void *d_map = nullptr; size_t cap_map = 0;
   void *d_codes = nullptr; size_t cap_codes = 0;
   void *h_codes = nullptr; size_t cap_hcodes = 0;  // pinned staging of the DevCode array
@@ -89,7 +90,7 @@ class Context {
   static Context *get(int *err);
   int device = 0;
   int sm_count = 0;
-  int triage_bps = 1, search_bps = 1;
+  int decode_bps = 1;  // resident decode-kernel blocks per SM
   unsigned long long *d_ncr = nullptr;
   int pageable_access = 0;
 
@@ -123,7 +124,7 @@ struct BatchRequest {
 };
 
 struct BatchTiming {
-  float h2d_ms = 0, triage_ms = 0, search_ms = 0, d2h_ms = 0;
+  float h2d_ms = 0, reset_ms = 0, decode_ms = 0, d2h_ms = 0;
   int rounds = 0;
 };
 
@@ -131,7 +132,8 @@ struct BatchTiming {
 struct Tuning {
   int light_max_log2 = 12;
   int tile_k = 4;
-  int search_grid_mult = 0;  // CTAs per SM of the search kernel; 0: occupancy maximum
+  int search_grid_mult = 0;  // CTAs per SM of the decode kernel; 0: occupancy maximum
+  int fast = 1;              // settle shots 32 at a time before the per-shot path (GRAND_FAST)
   int zero_copy = 1;         // read records / write results in the caller's host memory
                              // when the device can access pageable memory (GRAND_ZERO_COPY)
 };
@@ -141,8 +143,12 @@ Tuning &tuning();  // process defaults (GRAND_LIGHT_LOG2, GRAND_TILE_K, GRAND_SE
 int run_batch(Context *ctx, Workspace *ws, const BatchRequest &req, BatchTiming *timing,
               const Tuning *tn = nullptr);
 
-// Enqueue one launch of the pipeline (counter reset, triage, search) on s.
+// Enqueue one decoding launch (control-word reset, decode kernel) on s.
 cudaError_t launch_pipeline(const Context *ctx, const DevBatch &b, const Tuning &tn,
                             cudaStream_t s, cudaEvent_t mid = nullptr);
+
+// Blocks of the decode kernel per SM for a tuning (CTAs-per-SM override or the
+// occupancy maximum).
+int decode_blocks_per_sm(int occupancy_bps, const Tuning &tn);
 
 }  // namespace grand

@@ -10,15 +10,71 @@
 
 namespace grand {
 
-constexpr int kTriageWarps = 4;                 // warps per triage block
+constexpr int kDecodeWarps = 4;                 // warps per block of the decode kernel
 constexpr int kLightTam = 96;                   // largest active set the triage warp searches
 constexpr int kLightWords = kLightTam * 8;      // its staged column words (nwp <= 8)
-constexpr int kSearchThreads = 256;
-constexpr int kSearchWarps = kSearchThreads / 32;
 constexpr int kWarpStage = 1280;  // per search warp: staged column sketches, or the Job at its end
 constexpr int kTilesPerFetch = 4;  // most tiles a search warp draws at once
 constexpr int kRunKK = 8;       // prefixes per lane in a run tile (search kernel)
 constexpr int kRunKKLight = 4;  // the same inside the triage warp's light search
+
+// Per-warp shared memory of the decode kernel.  A warp does one kind of work at
+// a time and reuses the same bytes for it: a shot's triage (the fields below), a
+// chunk's classification (FastArea, grand_triage.cuh) or search tiles (the first
+// kWarpStage words hold the staged sketches or a Job being finished, then the
+// syndrome and the degeneracy delta).
+struct alignas(128) WarpArea {
+  uint32_t cols[kLightWords];
+  uint32_t hcols[kLightTam];
+  float llr[kLightTam];
+  int pos[kLightTam];
+  int tmp[kLightTam];
+  uint32_t sw[kMaxRows / 32];
+  uint32_t eb[kMaxCols / 32];
+  uint32_t am[kMaxIters][kMaxCols / 32];
+  uint32_t delta[kMaxCols / 32];
+  Job job;
+};
+
+// Planner state of one shot (resumable walk over upstream's iteration loop).
+struct PlanState {
+  int i, tam, tam_old, passes;
+  unsigned long long gbase;
+};
+
+// Bounded waits.  A warp that waits for another warp's progress sleeps between
+// polls, longer as the wait goes on; after kWaitPolls polls it gives up and
+// raises kStatusWaitLimit (never expected: every wait is for a warp that is
+// running and waits for nothing this warp holds).
+constexpr int kWaitPolls = 1 << 21;
+
+__device__ __forceinline__ void nap(int polls) {
+#ifdef GRAND_HOST_EMULATION
+  grand_host_nap(polls);
+#else
+  __nanosleep(polls < 8 ? 32u : (polls < 64 ? 256u : 1000u));
+#endif
+}
+
+// Lane 0 only.  Counter `ctr` is advanced in reservation order: once it holds
+// `mine` (every earlier reservation published) this warp sets it to `next`.  The
+// fence orders the warp's writes (made visible to lane 0 by the caller's
+// __syncwarp after each lane fenced its own) before the counter.
+__device__ __forceinline__ void publish_in_order(const DevBatch &b, int ctr,
+                                                 unsigned long long mine,
+                                                 unsigned long long next) {
+  __threadfence();
+  volatile unsigned long long *c = b.counters + ctr;
+  for (int polls = 0; *c != mine; ++polls) {
+    if (polls >= kWaitPolls) {
+      atomicOr(b.status, kStatusWaitLimit);
+      break;
+    }
+    nap(polls);
+  }
+  *c = next;
+  __threadfence();
+}
 
 // ---------------------------------------------------------------------------
 // Result writer shared by the light path and the search kernel (one warp).

@@ -8,8 +8,7 @@
 // cudaMalloc on first use (and grow them); this one keeps everything it needs
 // beyond the caller's inputs and outputs in one fixed, file-scope device array.
 //
-// The batch runs through the same triage and search kernels as the other entry
-// points.  Only the place their scratch lives differs: the binomial table, the
+// The batch runs through the same decode kernel as the other entry points.  Only the place their scratch lives differs: the binomial table, the
 // packed columns, the code descriptor, the counters, the job table and the
 // scratch arena are carved out of g_noalloc_scratch.
 #include <cuda_runtime.h>
@@ -40,7 +39,8 @@ constexpr size_t kOffSmall = align256(kOffHcol + sizeof(uint32_t) * kNaMaxCols);
 constexpr size_t kOffDeferred = align256(kOffSmall + 256);
 constexpr size_t kOffMap = align256(kOffDeferred + sizeof(int) * kNaChunk);     // re-run list
 constexpr size_t kOffMapCount = align256(kOffMap + sizeof(int) * kNaChunk);     // its length
-constexpr size_t kOffJobs = align256(kOffMapCount + 256);
+constexpr size_t kOffQueue = align256(kOffMapCount + 256);                       // slow queue
+constexpr size_t kOffJobs = align256(kOffQueue + sizeof(int) * kNaChunk);
 constexpr size_t kOffArena = align256(kOffJobs + sizeof(Job) * kNaChunk);
 constexpr size_t kScratchBytes = align256(kOffArena + sizeof(uint32_t) * kNaArenaWords);
 
@@ -139,7 +139,7 @@ __global__ void noalloc_clear_kernel(const int *map, int count, GrandDecoderResu
 
 std::mutex g_mu;
 unsigned char *g_base[64] = {};  // device address of g_noalloc_scratch per device
-int g_sms[64] = {}, g_tbps[64] = {}, g_sbps[64] = {};
+int g_sms[64] = {}, g_bps[64] = {};
 
 }  // namespace
 }  // namespace grand
@@ -194,9 +194,9 @@ extern "C" int grand_decode_cc_noalloc(const int *d_H, int n, int m, const int *
                 cudaGetErrorString(e));
         return GRAND_ERR_CUDA;
       }
-      int sms = 0, tb = 0, sb = 0;
+      int sms = 0, bps = 0;
       e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-      if (e == cudaSuccess) e = occupancy(&tb, &sb);
+      if (e == cudaSuccess) e = decode_occupancy(&bps);
       if (e == cudaSuccess) {
         noalloc_ncr_kernel<<<(kMaxTam + 256) / 256, 256, 0, s>>>(
             reinterpret_cast<unsigned long long *>((unsigned char *)ptr + kOffNcr));
@@ -208,8 +208,7 @@ extern "C" int grand_decode_cc_noalloc(const int *d_H, int n, int m, const int *
         return GRAND_ERR_CUDA;
       }
       g_sms[dev] = sms;
-      g_tbps[dev] = tb > 0 ? tb : 1;
-      g_sbps[dev] = sb > 0 ? sb : 1;
+      g_bps[dev] = bps > 0 ? bps : 1;
       g_base[dev] = (unsigned char *)ptr;
     }
     base = g_base[dev];
@@ -249,10 +248,8 @@ extern "C" int grand_decode_cc_noalloc(const int *d_H, int n, int m, const int *
   if (e == cudaSuccess) e = cudaMemsetAsync(base + kOffSmall + 128, 0, 128, s);
 
   const Tuning &tn = tuning();
-  // the search kernel's CTAs per SM as the regular entry points choose them
-  const int per_sm = tn.search_grid_mult ? (tn.search_grid_mult < g_sbps[dev] ? tn.search_grid_mult
-                                                                               : g_sbps[dev])
-                                         : g_sbps[dev];
+  // the decode kernel's CTAs per SM as the regular entry points choose them
+  const int per_sm = decode_blocks_per_sm(g_bps[dev], tn);
   int *map = reinterpret_cast<int *>(base + kOffMap);
   int *map_count = reinterpret_cast<int *>(base + kOffMapCount);
   unsigned st = 0;       // status bits of every round of every chunk
@@ -273,6 +270,8 @@ extern "C" int grand_decode_cc_noalloc(const int *d_H, int n, int m, const int *
     b.scratch = reinterpret_cast<uint32_t *>(base + kOffArena);
     b.scratch_words = kNaArenaWords;
     b.deferred = reinterpret_cast<int *>(base + kOffDeferred);
+    b.queue = reinterpret_cast<int *>(base + kOffQueue);
+    b.fast = tn.fast;
     b.light_max_log2 = tn.light_max_log2;
     b.tile_k = tn.tile_k;
     // Rounds: all of the chunk's shots, then, while some heavy shots found the
@@ -283,12 +282,9 @@ extern "C" int grand_decode_cc_noalloc(const int *d_H, int n, int m, const int *
     for (int round = 0; e == cudaSuccess; ++round) {
       b.num_shots = todo;
       b.shot_map = round == 0 ? nullptr : map;
-      // counters (job, tile, arena, shot) and status restart for every round
+      // control words and status restart for every round
       e = cudaMemsetAsync(base + kOffSmall, 0, 256, s);
-      const int tgrid_max = g_sms[dev] * g_tbps[dev];
-      const int tgrid = (todo + 3) / 4 < tgrid_max ? (todo + 3) / 4 : tgrid_max;
-      if (e == cudaSuccess) e = launch_triage(b, tgrid > 0 ? tgrid : 1, s);
-      if (e == cudaSuccess) e = launch_search(b, g_sms[dev] * per_sm, s);
+      if (e == cudaSuccess) e = launch_decode(b, g_sms[dev] * per_sm, s);
       unsigned rs = 0;
       if (e == cudaSuccess)
         e = cudaMemcpyAsync(&rs, base + kOffSmall + 128, sizeof(unsigned), cudaMemcpyDeviceToHost, s);

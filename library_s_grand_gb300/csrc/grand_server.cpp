@@ -148,6 +148,8 @@ cudaError_t start_slot(GrandServer *S, SrvSlot *sl) {
   b.scratch = sl->d_scratch;
   b.scratch_words = kSrvArenaWords;
   b.deferred = sl->d_deferred;
+  b.queue = sl->d_deferred + S->max_shots;
+  b.fast = e->tn.fast;
   b.light_max_log2 = e->tn.light_max_log2;
   b.tile_k = e->tn.tile_k;
   for (const DevCode &c : e->codes) b.has_ml |= c.variant == kMl;
@@ -275,7 +277,7 @@ int grand_server_create(GrandEngine *e, int slots, int max_shots, size_t budget,
   const size_t jobb = align256(sizeof(Job) * max_shots);
   const size_t arena = align256(sizeof(uint32_t) * kSrvArenaWords);
   const size_t smallb = 256;
-  const size_t defb = align256(sizeof(int) * max_shots);
+  const size_t defb = align256(2 * sizeof(int) * max_shots);  // re-run flags, then the slow queue
   const size_t per_slot = rec + offb + codeb + resb + jobb + arena + smallb + defb;
   size_t free_b = 0, total_b = 0;
   if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {

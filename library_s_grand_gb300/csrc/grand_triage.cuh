@@ -1,31 +1,29 @@
-// grand_triage.cu -- kernel 1 of a decoding launch (sm_103a).
+// grand_triage.cuh -- the per-shot work of a decoding launch (sm_103a), run by
+// the warps of the persistent decode kernel (grand_decode.cuh).
 //
-// triage_kernel (one warp per shot, grid-stride over the batch)
-//   packs the shot's int32 record into bits, forms the syndrome, computes the
+// classify_chunk (32 launch slots, one lane per shot)
+//   packs the 32 shots' records with coalesced ballots, forms each syndrome and
+//   settles the common shots outright: an empty syndrome (grand_decoder.cu:1223-1241),
+//   and a first threshold iteration with one active position whose column equals
+//   the syndrome (weight-1 match, 1 candidate tested).  The others go to the slow
+//   queue.
+//
+// triage_shot (one warp per shot)
+//   packs the shot's record into bits, forms the syndrome, computes the
 //   flagged-check count of every column (popc(col & s), upstream
 //   grand_decoder.cu:67-81 / 352-374, with the irregular offset of :406-416),
 //   the active sets of the <= 3 threshold iterations (:1284-1290, :495-504),
 //   the upstream active-set cap and mode rules (:1296, :1327, :1550-1554), and
 //   the weight blocks each searched iteration enumerates.  The iterations are
 //   searched in upstream order by the same warp while each fits the light
-//   budget; the first larger one and those after it become a Job for the
-//   persistent search kernel (grand_search.cu).
+//   budget; the first larger one and those after it become a Job whose tiles
+//   every warp of the launch searches (grand_search.cuh).
+#pragma once
+
 #include "grand_kernels.cuh"
 
 namespace grand {
 
-struct alignas(16) WarpArea {
-  uint32_t cols[kLightWords];
-  uint32_t hcols[kLightTam];
-  float llr[kLightTam];
-  int pos[kLightTam];
-  int tmp[kLightTam];
-  uint32_t sw[kMaxRows / 32];
-  uint32_t eb[kMaxCols / 32];
-  uint32_t am[kMaxIters][kMaxCols / 32];
-  uint32_t delta[kMaxCols / 32];
-  Job job;
-};
 
 // ---------------------------------------------------------------------------
 // Planning: the threshold iterations and their weight blocks (lane 0 only).
@@ -35,12 +33,8 @@ struct alignas(16) WarpArea {
 // fields of an exhausted loop and returns 0.  Shots usually resolve in their
 // first searched iteration, so later iterations are only planned when needed.
 // ---------------------------------------------------------------------------
-struct PlanState {
-  int i, tam, tam_old, passes;
-  unsigned long long gbase;
-};
 
-__device__ int plan_next(const DevCode &cd, int tam0, int tam1, int tam2, int L, int tile_k, Job &J,
+static __device__ int plan_next(const DevCode &cd, int tam0, int tam1, int tam2, int L, int tile_k, Job &J,
                          PlanState &P) {
   while (P.i < L) {
     const int i = P.i++;
@@ -209,24 +203,6 @@ __device__ __forceinline__ int pack_ballots(const int *p, int n, uint32_t *dst) 
   return total;
 }
 
-// Ask L2 for the record of batch slot `slot` (the warp's next shot) while the
-// current one is processed: one prefetch per 128-byte line, all inside the record.
-__device__ __forceinline__ void prefetch_next_record(const DevBatch &b, int slot) {
-  if (slot >= b.num_shots) return;
-  const int lane = threadIdx.x & 31;
-  const int shot = b.shot_map ? b.shot_map[slot] : slot;
-  const int ci = b.shot_code ? b.shot_code[shot] : 0;
-  const int len = b.codes[ci].rec_len;
-  const char *p = reinterpret_cast<const char *>(
-      b.in + (b.in_off ? b.in_off[shot] : (long long)shot * len));
-  const int nbytes = len * 4;
-#ifndef GRAND_HOST_EMULATION  // a hint only: the host build of the kernels skips it
-  for (int o = lane * 128; o < nbytes; o += 32 * 128)
-    asm volatile("prefetch.global.L2 [%0];" ::"l"(p + o));
-  if (lane == 0 && nbytes > 0) asm volatile("prefetch.global.L2 [%0];" ::"l"(p + nbytes - 1));
-#endif
-}
-
 // ---------------------------------------------------------------------------
 // Small active sets: every subset as a bit mask.
 // ---------------------------------------------------------------------------
@@ -351,7 +327,7 @@ __device__ void small_iteration(const uint32_t *cols, const uint32_t *hcols, con
 // error rates): its only candidate is that column, weight 1, rank 0 of the
 // first weight-1 block, and it matches when the column equals the syndrome.
 // The same winner as the small-set path, without staging the iteration.
-__device__ void single_search(const DevCode &cd, Job &J, WarpArea &A, int ii, Winner &wn) {
+static __device__ void single_search(const DevCode &cd, Job &J, WarpArea &A, int ii, Winner &wn) {
   const int lane = threadIdx.x & 31;
   IterInfo &I = J.it[ii];
   int s = I.seg_lo;
@@ -502,22 +478,11 @@ __device__ void light_search(const DevBatch &b, const DevCode &cd, Job &J, WarpA
   }
 }
 
-// MLK = false: a build without the ML paths (smaller code) for batches without ML codes.
+// The full per-shot path: one warp, launch slot `slot`.  P is the warp's planner state.
 template <bool MLK>
-__global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
-  __shared__ WarpArea areas[kTriageWarps];
+__device__ void triage_shot(const DevBatch &b, int slot, WarpArea &A, PlanState &P) {
   const int lane = threadIdx.x & 31;
-  const int wib = threadIdx.x >> 5;
-  WarpArea &A = areas[wib];
-
-  // Shots are drawn one at a time from a batch-wide counter, so a warp that
-  // drew cheap shots keeps drawing while another works through an expensive
-  // one.  The next draw is issued at the top of each shot and read at its end.
-  unsigned long long nxt = 0;
-  if (lane == 0) nxt = atomicAdd(&b.counters[3], 1ull);
-  for (int slot = __shfl_sync(kFull, (int)nxt, 0); slot < b.num_shots;
-       slot = __shfl_sync(kFull, (int)nxt, 0)) {
-    if (lane == 0) nxt = atomicAdd(&b.counters[3], 1ull);
+  {
     const unsigned long long t_start = global_ns();
     const int shot = b.shot_map ? b.shot_map[slot] : slot;
     const int ci = b.shot_code ? b.shot_code[shot] : 0;
@@ -551,7 +516,6 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) original_weight += __shfl_xor_sync(kFull, original_weight, o);
       if (cd.input_kind != kInErrors) original_weight = 0;
-      prefetch_next_record(b, __shfl_sync(kFull, (int)nxt, 0));
       __syncwarp();
       if (cd.input_kind == kInErrors) {
         for (int q = 0; q < cd.mw && original_weight != 0; ++q) {
@@ -567,7 +531,6 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
       }
     } else if (cd.input_kind == kInErrors) {
       original_weight = pack_ballots(rec, cd.m, A.eb);
-      prefetch_next_record(b, __shfl_sync(kFull, (int)nxt, 0));
       __syncwarp();
       // s = XOR of the columns of the supplied error (grand_decoder.cu:476-486);
       // an error-free record (most shots at low error rates) skips the walk
@@ -584,7 +547,6 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
       if (cd.family == kDem)
         pack_ballots(b.in_log ? b.in_log + (size_t)shot * cd.n_logicos : rec + cd.R, cd.n_logicos,
                      A.eb);
-      prefetch_next_record(b, __shfl_sync(kFull, (int)nxt, 0));
       __syncwarp();
       s_lane = lane < cd.nw ? A.sw[lane] : 0u;
     }
@@ -605,7 +567,7 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
         for (int j = lane; j < cd.n_logicos; j += 32) b.dec_log[(size_t)shot * cd.n_logicos + j] = 0;
       if (b.deferred && lane == 0) b.deferred[shot] = 0;
       __syncwarp();
-      continue;
+      return;
     }
 
     // Sketch of the syndrome (XOR of the row hashes of its set rows), read by
@@ -677,8 +639,6 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
         }
       }
     }
-    __shared__ PlanState plans[kTriageWarps];
-    PlanState &P = plans[wib];
     if (lane == 0) {
       J.n_it = 0;
       J.nseg = 0;
@@ -739,7 +699,7 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
       finish_shot(b, cd, J, shot, wn, A.eb, A.delta);
       if (b.deferred && lane == 0) b.deferred[shot] = 0;
       __syncwarp();
-      continue;
+      return;
     }
 
     // ---- heavy: publish a Job ------------------------------------------------
@@ -758,6 +718,8 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
         words += (2ull * (unsigned long long)J.it[S.iter].tam + 3ull) & ~3ull;  // run-tile table
     }
     words += 128;  // supplied bits
+    // whole 128-byte lines, so no line is shared with another Job's data
+    words = (words + 31ull) & ~31ull;
     unsigned long long off = 0, jslot = 0, tbase = 0, ntl = 0;
     int ok = 1;
     if (lane == 0) {
@@ -779,7 +741,7 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
     if (!ok) {
       if (lane == 0 && b.deferred) b.deferred[shot] = 1;
       __syncwarp();
-      continue;
+      return;
     }
     off = __shfl_sync(kFull, off, 0);
     uint32_t *sp = b.scratch + off;
@@ -849,19 +811,30 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
         S.tile_lo = ntl;
         ntl += S.njt;
       }
-      const unsigned long long old = atomicAdd(&b.counters[0], (1ull << 40) | ntl);
+      // Reserve a job slot and the next ntl tiles (job table permitting); a
+      // reservation that does not fit takes nothing.
+      ok = 0;
+      unsigned long long old =
+          *reinterpret_cast<volatile unsigned long long *>(&b.counters[kCtrJobsReserved]);
+      for (int guard = 0; guard < (1 << 16) && (old >> 40) < (unsigned long long)b.max_jobs;
+           ++guard) {
+        const unsigned long long seen =
+            atomicCAS(&b.counters[kCtrJobsReserved], old, old + (1ull << 40) + ntl);
+        if (seen == old) {
+          ok = 1;
+          break;
+        }
+        old = seen;
+      }
+      if (!ok) atomicOr(b.status, kStatusJobOverflow);
       jslot = old >> 40;
       tbase = old & ((1ull << 40) - 1ull);
-      if (jslot >= (unsigned long long)b.max_jobs) {
-        ok = 0;
-        atomicOr(b.status, kStatusJobOverflow);
-      }
     }
     ok = __shfl_sync(kFull, ok, 0);
     if (!ok) {
       if (lane == 0 && b.deferred) b.deferred[shot] = 1;
       __syncwarp();
-      continue;
+      return;
     }
     jslot = __shfl_sync(kFull, jslot, 0);
     tbase = __shfl_sync(kFull, tbase, 0);
@@ -883,26 +856,350 @@ __global__ void __launch_bounds__(kTriageWarps * 32) triage_kernel(DevBatch b) {
     }
     if (lane == 0 && b.deferred) b.deferred[shot] = 0;
     __syncwarp();
+    // Jobs become visible to the searching warps in reservation order, each only
+    // once it is fully written: wait for the Jobs reserved before this one.
+    if (lane == 0)
+      publish_in_order(b, kCtrJobsPublished, (jslot << 40) | tbase, ((jslot + 1ull) << 40) | (tbase + ntl));
+    __syncwarp();
   }
 }
 
+
 // ---------------------------------------------------------------------------
-// Host-callable launcher.
+// Classification of 32 launch slots, one lane per shot.
 // ---------------------------------------------------------------------------
-#ifndef GRAND_HOST_EMULATION  // launchers: device builds only
-cudaError_t launch_triage(const DevBatch &b, int grid, cudaStream_t s) {
-  if (b.has_ml) triage_kernel<true><<<grid, kTriageWarps * 32, 0, s>>>(b);
-  else triage_kernel<false><<<grid, kTriageWarps * 32, 0, s>>>(b);
-  return cudaGetLastError();
+constexpr int kFastWords = 4;       // syndrome / logical words a lane keeps (R, n_logicos <= 128)
+constexpr int kFastErrWords = 16;   // error-record words a lane walks (m <= 512)
+constexpr int kFastBallots = 512;   // ballot words of a chunk's records (16384 int32 entries)
+constexpr int kFastLogBallots = 128;  // ballot words of a chunk's separate logical entries
+
+// classify_chunk's part of the WarpArea.
+struct FastArea {
+  uint32_t bits[kFastBallots + 1];      // bit e: entry e of the chunk's records (flat)
+  uint32_t lbits[kFastLogBallots + 1];  // the same for DEM logicals kept in their own array
+  uint32_t res[32][18];                 // result words, one row per lane
+};
+static_assert(sizeof(FastArea) <= sizeof(WarpArea), "FastArea must fit the warp's area");
+
+// bits[k] = ballot(p[32k + lane] != 0) for the n entries at p (bits past n are 0),
+// sixteen words' loads issued before their ballots; bits[ceil(n/32)] = 0.
+__device__ __forceinline__ void flat_ballots(const int *p, int n, uint32_t *bits) {
+  const int lane = threadIdx.x & 31;
+  const int nwords = (n + 31) >> 5;
+  for (int k0 = 0; k0 < nwords; k0 += 16) {
+    int v[16];
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      const int e = (k0 + u) * 32 + lane;
+      v[u] = e < n ? __ldcg(p + e) : 0;  // kept in L2: the slow path may read it again
+    }
+    uint32_t mine = 0u;
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      const uint32_t w = __ballot_sync(kFull, v[u] != 0);
+      mine = lane == u ? w : mine;
+    }
+    if (lane < 16 && k0 + lane < nwords) bits[k0 + lane] = mine;
+  }
+  if (lane == 0) bits[nwords] = 0u;
 }
 
-int triage_warps_per_block() { return kTriageWarps; }
-
-cudaError_t triage_occupancy(int *blocks_per_sm) {
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, triage_kernel<true>,
-                                                       kTriageWarps * 32, 0);
+// Word q of the nbits-entry bit vector that starts at entry `off` of a flat
+// ballot array (entries past nbits masked off).
+__device__ __forceinline__ uint32_t flat_word(const uint32_t *bits, int off, int q, int nbits) {
+  const int e = off + 32 * q;
+  uint32_t w = __funnelshift_r(bits[e >> 5], bits[(e >> 5) + 1], e & 31);
+  const int rem = nbits - 32 * q;
+  if (rem < 32) w &= (1u << rem) - 1u;
+  return w;
 }
 
-#endif
+// Upstream's planner (grand_decoder.cu:1284-1296, 1550-1554, 754-786) for a first
+// threshold iteration with one active position: is it searched, and with a
+// weight-1 block (its only candidate)?  *gpu: the branch upstream takes.
+__device__ __forceinline__ bool one_position_searched(const DevCode &cd, bool *gpu) {
+  if (cd.family == kDem && 1 > cd.cap) return false;  // the cap replaces the set by an empty one
+  const bool g = (1 > cd.thr && 1 <= cd.cap && cd.mode == 1) || cd.mode == 0;
+  const bool c = !g && ((1 <= cd.thr && cd.mode == 1) || cd.mode == -1);
+  if (!g && !c) return false;
+  *gpu = g;
+  if (cd.variant != kProb) return true;  // weights 1..min(W, 1)
+  int mi = cd.n_masks - 1;
+  for (int q = 0; q < cd.n_masks; ++q)
+    if (1 <= cd.mask_tam_upper[q]) {
+      mi = q;
+      break;
+    }
+  for (int k = 0; k < cd.num_phases; ++k)
+    if (cd.mask_order[mi][k] == 0) return true;  // phase 0 lists weight 1
+  return false;
+}
+
+// Settles the shots of launch slots 32*chunk .. 32*chunk+31 that need no search
+// -- an empty syndrome, or a first iteration with one active position whose
+// column equals the syndrome -- and appends the others to the slow queue.  The
+// results are exactly those of triage_shot: the one position is the only
+// candidate of the iteration (found at weight 1, rank 0; one candidate counted
+// on either branch, hibrido 0 / -1), and its active set is the set of nonzero
+// columns contained in the syndrome (flagged-check count = column weight, for
+// 0/1 matrices regular or not), found through the columns grouped by their
+// lowest row.  Shots the lanes cannot settle here (ML codes, supplied errors
+// that differ from the match, wide codes, records that are not back to back)
+// take the slow path.
+template <bool MLK>
+__device__ void classify_chunk(const DevBatch &b, int chunk, WarpArea &A) {
+  FastArea &F = *reinterpret_cast<FastArea *>(&A);
+  const int lane = threadIdx.x & 31;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  const int slot = chunk * 32 + lane;
+  const bool valid = slot < b.num_shots;
+  const unsigned long long t_start = global_ns();
+  const int shot = valid ? (b.shot_map ? b.shot_map[slot] : slot) : 0;
+  const int ci = (valid && b.shot_code) ? b.shot_code[shot] : 0;
+  const DevCode &cd = b.codes[ci];
+  const bool errs = cd.input_kind == kInErrors;
+  const bool dem = cd.family == kDem;
+  const int nbits = errs ? cd.m : cd.R;       // entries of the record's leading bit vector
+  const int nwords = (nbits + 31) >> 5;
+  bool ok = valid && cd.nw <= kFastWords && (!errs || nwords <= kFastErrWords) &&
+            (!dem || cd.nlw <= kFastWords);
+  const long long rbase = valid ? (b.in_off ? b.in_off[shot] : (long long)shot * cd.rec_len) : 0;
+
+  uint32_t s[kFastWords] = {0u, 0u, 0u, 0u};
+  uint32_t lg[kFastWords] = {0u, 0u, 0u, 0u};
+  int ow = 0, epos = -1;
+
+  // ---- the records: int32 entries through coalesced ballots over the chunk's
+  //      back-to-back records, bit-packed words read directly -----------------
+  const bool packed = cd.packed != 0;
+  const bool any_int = __any_sync(kFull, valid && !packed);
+  if (any_int) {
+    // entries this lane's shot occupies in b.in, and whether the chunk's
+    // records lie back to back in slot order
+    const int rlen = (dem && !b.in_log) ? cd.R + cd.n_logicos : nbits;
+    const long long nb = __shfl_down_sync(kFull, rbase, 1);
+    const bool nv = __shfl_down_sync(kFull, valid ? 1 : 0, 1) != 0;
+    const bool joined = !valid || lane == 31 || !nv || nb == rbase + rlen;
+    const long long first = __shfl_sync(kFull, rbase, 0);
+    long long end = valid ? rbase + rlen : first;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const long long u = __shfl_xor_sync(kFull, end, o);
+      end = u > end ? u : end;
+    }
+    bool flat = __all_sync(kFull, joined && !(valid && packed)) && end - first <= 32ll * kFastBallots;
+    // DEM logicals in their own array: back to back by shot as well
+    const bool sep_log = dem && b.in_log && valid;
+    const bool any_sep = __any_sync(kFull, sep_log);
+    long long lbase = 0, lfirst = 0, lend = 0;
+    if (flat && any_sep) {
+      lbase = sep_log ? (long long)shot * cd.n_logicos : 0;
+      const long long lnb = __shfl_down_sync(kFull, lbase, 1);
+      const bool ljoined = !valid || lane == 31 || !nv || lnb == lbase + cd.n_logicos;
+      lfirst = __shfl_sync(kFull, lbase, 0);
+      lend = valid ? lbase + cd.n_logicos : lfirst;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const long long u = __shfl_xor_sync(kFull, lend, o);
+        lend = u > lend ? u : lend;
+      }
+      flat = __all_sync(kFull, ljoined && sep_log == (valid && dem)) &&
+             lend - lfirst <= 32ll * kFastLogBallots;
+    }
+    if (flat) {
+      flat_ballots(b.in + first, (int)(end - first), F.bits);
+      if (any_sep) flat_ballots(b.in_log + lfirst, (int)(lend - lfirst), F.lbits);
+      __syncwarp();
+      if (ok) {
+        const int off = (int)(rbase - first);
+        if (errs) {
+          for (int q = 0; q < nwords; ++q) {
+            uint32_t w = flat_word(F.bits, off, q, nbits);
+            ow += __popc(w);
+            while (w) {
+              const int c = q * 32 + __ffs(w) - 1;
+              w &= w - 1u;
+              epos = c;
+#pragma unroll
+              for (int k = 0; k < kFastWords; ++k)
+                if (k < cd.nw) s[k] ^= __ldg(cd.cols + (size_t)c * cd.nwp + k);
+            }
+          }
+        } else {
+#pragma unroll
+          for (int k = 0; k < kFastWords; ++k)
+            if (k < cd.nw) s[k] = flat_word(F.bits, off, k, cd.R);
+          if (dem) {
+#pragma unroll
+            for (int k = 0; k < kFastWords; ++k)
+              if (k < cd.nlw)
+                lg[k] = b.in_log ? flat_word(F.lbits, (int)(lbase - lfirst), k, cd.n_logicos)
+                                 : flat_word(F.bits, off + cd.R, k, cd.n_logicos);
+          }
+        }
+      }
+    } else {
+      ok = ok && packed;  // int32 records that are not back to back: slow path
+    }
+  }
+  if (ok && packed) {
+    const uint32_t *rw = reinterpret_cast<const uint32_t *>(b.in) + rbase;
+    if (errs) {
+      for (int q = 0; q < nwords; ++q) {
+        uint32_t w = __ldcg(rw + q);
+        if (q == nwords - 1 && (nbits & 31)) w &= (1u << (nbits & 31)) - 1u;
+        ow += __popc(w);
+        while (w) {
+          const int c = q * 32 + __ffs(w) - 1;
+          w &= w - 1u;
+          epos = c;
+#pragma unroll
+          for (int k = 0; k < kFastWords; ++k)
+            if (k < cd.nw) s[k] ^= __ldg(cd.cols + (size_t)c * cd.nwp + k);
+        }
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < kFastWords; ++k)
+        if (k < cd.nw) {
+          uint32_t w = __ldcg(rw + k);
+          if (k == cd.nw - 1 && (cd.R & 31)) w &= (1u << (cd.R & 31)) - 1u;
+          s[k] = w;
+        }
+      if (dem) {
+        const uint32_t *lw = b.in_log ? reinterpret_cast<const uint32_t *>(b.in_log) + (size_t)shot * cd.nlw
+                                      : rw + cd.nw;
+#pragma unroll
+        for (int k = 0; k < kFastWords; ++k)
+          if (k < cd.nlw) {
+            uint32_t w = __ldcg(lw + k);
+            if (k == cd.nlw - 1 && (cd.n_logicos & 31)) w &= (1u << (cd.n_logicos & 31)) - 1u;
+            lg[k] = w;
+          }
+      }
+    }
+  }
+  if (!errs) ow = 0;
+
+  // ---- settle: empty syndrome, or a one-position first iteration matched ----
+  const bool empty = ok && (s[0] | s[1] | s[2] | s[3]) == 0u;
+  bool found = false, gpu = false;
+  int pos = -1, deg = 0, iseq = 0;
+  if (ok && !empty && cd.variant != kMl && cd.lowstart && cd.binary && cd.max_soma >= 1 &&
+      one_position_searched(cd, &gpu)) {
+    // the first iteration's active set: nonzero columns contained in s, each
+    // reached once through its lowest row (which s must contain)
+    int tam0 = 0;
+#pragma unroll
+    for (int q = 0; q < kFastWords; ++q) {
+      uint32_t rows = q < cd.nw ? s[q] : 0u;
+      while (rows && tam0 < 2) {
+        const int r = q * 32 + __ffs(rows) - 1;
+        rows &= rows - 1u;
+        const int i1 = __ldg(cd.lowstart + r + 1);
+        for (int i = __ldg(cd.lowstart + r); i < i1 && tam0 < 2; ++i) {
+          const int c = __ldg(cd.lowcols + i);
+          bool inside = true;
+#pragma unroll
+          for (int k = 0; k < kFastWords; ++k)
+            if (k < cd.nw) inside = inside && (__ldg(cd.cols + (size_t)c * cd.nwp + k) & ~s[k]) == 0u;
+          if (inside) {
+            ++tam0;
+            pos = c;
+          }
+        }
+      }
+    }
+    if (tam0 == 1) {
+      found = true;
+#pragma unroll
+      for (int k = 0; k < kFastWords; ++k)
+        if (k < cd.nw) found = found && __ldg(cd.cols + (size_t)pos * cd.nwp + k) == s[k];
+    }
+    if (found) {
+      if (!dem && errs) {
+        iseq = (ow == 1 && epos == pos) ? 1 : 0;
+        deg = 1;
+        found = iseq != 0;  // a different supplied error needs the degeneracy test
+      } else if (dem) {
+        deg = 1;
+#pragma unroll
+        for (int k = 0; k < kFastWords; ++k)
+          if (k < cd.nlw && __ldg(cd.lcols + (size_t)pos * cd.nlw + k) != lg[k]) deg = 0;
+      }
+    }
+  }
+  const bool done = empty || found;
+  if (!found) pos = -1;
+
+  // ---- results of the settled shots ----------------------------------------
+  if (done) {
+    const unsigned long long now = global_ns();
+    uint32_t *r = F.res[lane];
+#pragma unroll
+    for (int w = 0; w < 18; ++w) r[w] = 0u;
+    r[2] = (uint32_t)ow;
+    if (empty) {
+      r[8] = (uint32_t)-2;
+    } else {
+      const unsigned long long half = t_start + (now - t_start) / 2;  // counts ~ half the time
+      const double t_sum = 1e-6 * (double)(half - t_start);
+      const double t_search = 1e-6 * (double)(now - half);
+      const double t_all = 1e-6 * (double)(now - t_start);
+      r[0] = 1u;
+      r[1] = 1u;
+      r[3] = (uint32_t)deg;
+      r[4] = (uint32_t)iseq;
+      r[5] = 1u;
+      r[6] = 1u;
+      r[8] = gpu ? 0u : (uint32_t)-1;
+      r[9] = 1u;
+      const unsigned long long a = (unsigned long long)__double_as_longlong(t_sum);
+      const unsigned long long bb = (unsigned long long)__double_as_longlong(t_search);
+      const unsigned long long d = (unsigned long long)__double_as_longlong(t_all);
+      r[10] = (uint32_t)a;
+      r[11] = (uint32_t)(a >> 32);
+      r[12] = (uint32_t)bb;
+      r[13] = (uint32_t)(bb >> 32);
+      r[16] = (uint32_t)d;
+      r[17] = (uint32_t)(d >> 32);
+    }
+    if (b.ml_cost) b.ml_cost[shot] = 0.0f;
+    if (b.deferred) b.deferred[shot] = 0;
+  }
+  __syncwarp();
+  const unsigned settled = __ballot_sync(kFull, done);
+  for (unsigned mm = settled; mm; mm &= mm - 1u) {
+    const int j = __ffs(mm) - 1;
+    const int sj = __shfl_sync(kFull, shot, j);
+    if (lane < 18) reinterpret_cast<uint32_t *>(b.results + sj)[lane] = F.res[j][lane];
+    if (b.dec_err || b.dec_log) {
+      const int cj = __shfl_sync(kFull, ci, j);
+      const int pj = __shfl_sync(kFull, pos, j);
+      const DevCode &cdj = b.codes[cj];
+      if (b.dec_err)
+        for (int c = lane; c < cdj.m; c += 32) b.dec_err[(size_t)sj * cdj.m + c] = c == pj ? 1 : 0;
+      if (b.dec_log && cdj.family == kDem)
+        for (int c = lane; c < cdj.n_logicos; c += 32)
+          b.dec_log[(size_t)sj * cdj.n_logicos + c] =
+              pj >= 0 ? (unsigned char)((__ldg(cdj.lcols + (size_t)pj * cdj.nlw + (c >> 5)) >> (c & 31)) & 1u)
+                      : 0;
+    }
+  }
+
+  // ---- the others: appended to the slow queue --------------------------------
+  const bool slow = valid && !done;
+  const unsigned sm = __ballot_sync(kFull, slow);
+  if (sm) {
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(&b.counters[kCtrQueueReserved], (unsigned long long)__popc(sm));
+    base = __shfl_sync(kFull, base, 0);
+    if (slow) b.queue[base + __popc(sm & lt_mask)] = slot;
+    __threadfence();
+    __syncwarp();
+    if (lane == 0) publish_in_order(b, kCtrQueuePublished, base, base + __popc(sm));
+  }
+  __syncwarp();
+}
 
 }  // namespace grand

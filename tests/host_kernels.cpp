@@ -1,13 +1,17 @@
-// Host build of the two decoding kernels (csrc/grand_triage.cu, grand_search.cu)
-// on emulated warps, for the CPU parity tests (tests/test_host_kernels.py).
+// Host build of the decode kernel (csrc/grand_decode.cuh with grand_triage.cuh
+// and grand_search.cuh) on emulated warps, for the CPU parity tests
+// (tests/test_host_kernels.py).
 //
-// Each kernel runs as one thread block: one host thread per lane, the lanes of
-// a warp meeting at a barrier in every warp collective (ballot, shuffles,
+// The kernel runs as one thread block: one host thread per lane, the lanes of a
+// warp meeting at a barrier in every warp collective (ballot, shuffles,
 // reductions, votes, __syncwarp), the block's __shared__ arrays as static
-// storage, device atomics as host atomics.  The kernels' code keeps its lanes
-// converged at every collective, so it runs here as on the GPU, the order of
-// the warps' work aside (which never changes a result: every search result is
-// an exact minimum).  Code tables are built as the library builds them.
+// storage, device atomics as host atomics, a nap as a yield.  The kernel's code
+// keeps its lanes converged at every collective, so it runs here as on the GPU,
+// the order of the warps' work aside (which never changes a result: every
+// search result is an exact minimum).  The block's warps classify, triage and
+// search as the GPU's do, waiting for one another's published work.  Code
+// tables are built as the library builds them.  GRAND_EMU_FAST=0 sends every
+// shot through the per-shot path.
 //
 // Usage: host_kernels DIR   reads DIR/params.txt, DIR/H.bin, DIR/rec.bin (int32
 // records) and, for a CSS code, DIR/Hother.bin (the other check matrix) or, for
@@ -122,6 +126,21 @@ static inline unsigned __reduce_max_sync(unsigned, unsigned x) {
     return r;
   });
 }
+template <class T>
+static inline T __shfl_down_sync(unsigned, T x, unsigned d) {
+  unsigned long long u = 0;
+  memcpy(&u, &x, sizeof(T));
+  return collective(u, [d](const unsigned long long *v, unsigned lane) {
+    T r;
+    memcpy(&r, &v[lane + d < 32 ? lane + d : lane], sizeof(T));
+    return r;
+  });
+}
+static inline unsigned __funnelshift_r(unsigned lo, unsigned hi, unsigned sh) {
+  const unsigned long long v = ((unsigned long long)hi << 32) | lo;
+  return (unsigned)(v >> (sh & 31));
+}
+static inline void grand_host_nap(int) { std::this_thread::yield(); }
 static inline int __clz(unsigned x) { return x ? __builtin_clz(x) : 32; }
 static inline int __ffs(unsigned x) { return __builtin_ffs((int)x); }
 static inline int __popc(unsigned x) { return __builtin_popcount(x); }
@@ -206,8 +225,7 @@ static inline void grand_host_cas128(unsigned long long *slot, unsigned long lon
 #endif
 
 #define GRAND_HOST_EMULATION 1
-#include "grand_triage.cu"
-#include "grand_search.cu"
+#include "grand_decode.cuh"
 
 using namespace grand;
 
@@ -249,7 +267,7 @@ struct Code {
   int family = 0, variant = 0, input_kind = 0, n = 0, m = 0, N = 0, W = 0, nl = 0, packed = 0;
   int light = 12, tile_k = 4, rec_len = 0, log_len = 0;
   std::vector<uint32_t> cols, hcol, rows, lcols;
-  std::vector<int> colw, pivrow;
+  std::vector<int> colw, pivrow, lowstart, lowcols;
   std::vector<float> llr;
   DevCode d;
 };
@@ -299,6 +317,24 @@ static bool load_code(const std::string &dir, Code &k) {
         k.cols[(size_t)c * nwp + (r >> 5)] |= 1u << (r & 31);
         k.hcol[c] ^= row_hash(r);
       }
+  // nonzero columns grouped by their lowest row, as the library builds them
+  std::vector<int> lowrow(m, -1);
+  for (int r = n - 1; r >= 0; --r)
+    for (int c = 0; c < m; ++c)
+      if (H[(size_t)r * m + c] != 0) lowrow[c] = r;
+  k.lowstart.assign(n + 1, 0);
+  for (int c = 0; c < m; ++c)
+    if (lowrow[c] >= 0) ++k.lowstart[lowrow[c] + 1];
+  for (int r = 0; r < n; ++r) k.lowstart[r + 1] += k.lowstart[r];
+  k.lowcols.assign(std::max(k.lowstart[n], 1), 0);
+  {
+    std::vector<int> fill(k.lowstart.begin(), k.lowstart.end() - 1);
+    for (int c = 0; c < m; ++c)
+      if (lowrow[c] >= 0) k.lowcols[fill[lowrow[c]]++] = c;
+  }
+  int binary = 1;
+  for (size_t i = 0; i < H.size(); ++i)
+    if (H[i] != 0 && H[i] != 1) binary = 0;
   int max_soma = 0, regular = 1;
   for (int c = 0; c < m; ++c) max_soma = std::max(max_soma, k.colw[c]);
   for (int c = 1; c < m; ++c)
@@ -359,6 +395,9 @@ static bool load_code(const std::string &dir, Code &k) {
   d.rref = k.rows.data();
   d.pivrow = k.pivrow.data();
   d.hcol = k.hcol.data();
+  d.binary = binary;
+  d.lowstart = k.lowstart.data();
+  d.lowcols = k.lowcols.data();
   return true;
 }
 
@@ -384,8 +423,9 @@ static unsigned run_batch(DevBatch &b, int N) {
   const unsigned long long scratch_words = 8ull << 20;
   static std::vector<uint32_t> scratch;
   scratch.assign(scratch_words, 0u);
-  static std::vector<int> deferred;
+  static std::vector<int> deferred, queue;
   deferred.assign(N, 0);
+  queue.assign(std::max(N, 1), -1);
   b.num_shots = N;
   b.ncr = ncr.data();
   b.jobs = jobs.data();
@@ -395,20 +435,20 @@ static unsigned run_batch(DevBatch &b, int N) {
   b.scratch = scratch.data();
   b.scratch_words = scratch_words;
   b.deferred = deferred.data();
-  run_block(kTriageWarps * 32, [&] {
-    if (b.has_ml) triage_kernel<true>(b);
-    else triage_kernel<false>(b);
-  });
-  run_block(kSearchThreads, [&] {
-    if (b.has_ml) search_kernel<true>(b);
-    else search_kernel<false>(b);
+  b.queue = queue.data();
+  const char *fe = getenv("GRAND_EMU_FAST");
+  b.fast = (fe && *fe == '0') ? 0 : 1;
+  run_block(kDecodeWarps * 32, [&] {
+    if (b.has_ml) decode_kernel<true>(b);
+    else decode_kernel<false>(b);
   });
   for (int i = 0; i < N; ++i)
     if (deferred[i]) {
       fprintf(stderr, "shot %d deferred (status %u)\n", i, *b.status);
       exit(3);
     }
-  printf("ok %d shots, %llu jobs, status %u\n", N, small[0] >> 40, *b.status);
+  printf("ok %d shots, %llu jobs, %llu slow, status %u\n", N, small[kCtrJobsPublished] >> 40,
+         small[kCtrSlowDone], *b.status);
   return *b.status;
 }
 

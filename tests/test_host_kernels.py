@@ -47,7 +47,7 @@ def _num_phases(W):  # upstream's phase count per max weight
 
 
 def _run(exe, d, H, Ho, records, errors_input, variant, cfg, masks, light, tile_k=4,
-         L=None, logicals=None, llr_path=None, packed=False):
+         L=None, logicals=None, llr_path=None, packed=False, fast=True):
     """CSS when L is None (Ho: the other check matrix), else DEM (L: m x n_logicos,
     logicals: the true flips).  Returns results, decoded errors, the emulator's
     log line and, for a DEM, decoded logical flips and ML costs."""
@@ -73,7 +73,8 @@ def _run(exe, d, H, Ho, records, errors_input, variant, cfg, masks, light, tile_
             shutil.copy(llr_path, os.path.join(d, "llr.txt"))
     else:
         np.ascontiguousarray(Ho, dtype=np.int32).tofile(os.path.join(d, "Hother.bin"))
-    out = subprocess.run([exe, d], capture_output=True, text=True, timeout=600)
+    env = dict(os.environ, GRAND_EMU_FAST="1" if fast else "0")
+    out = subprocess.run([exe, d], capture_output=True, text=True, timeout=600, env=env)
     assert out.returncode == 0, out.stderr + out.stdout
     res = np.fromfile(os.path.join(d, "res.bin"), dtype=capi.RESULT_DTYPE)
     dec = np.fromfile(os.path.join(d, "dec.bin"), dtype=np.uint8).reshape(N, m)
@@ -262,3 +263,70 @@ def test_largest_code_shapes(emulator, port, tmp_path):
     _compare(res, dec, pres, pdec)
     assert int((pres["found"] == 1).sum()) >= 55
     assert int(log.split()[3]) > 0, log  # the search kernel had Jobs
+
+
+def _slow(log):
+    """Shots the emulated launch sent through the per-shot path."""
+    return int(log.split()[5])
+
+
+@pytest.mark.parametrize("name,variant,cfg,masks", [
+    ("mode -1", 0, (3, 256, 0, 64, 10, -1), []),
+    ("mode 0", 0, (3, 256, 0, 64, 10, 0), []),
+    ("mode 1, one position above thr", 0, (3, 256, 0, 64, 0, 1), []),
+    ("mode 1, cap 0", 0, (3, 256, 0, 0, 0, 1), []),
+    ("mode 5", 0, (3, 256, 0, 64, 10, 5), []),
+    ("prob, small sets skip weight 1", 1, (3, 256, 0, 64, 10, -1),
+     [(1, 1, 2, 2, 0.5, 0.5, 0.0), (300, 0, 1, 2, 1.0, 0.0, 0.0)]),
+    ("prob, phase 0 listed second", 1, (3, 256, 0, 64, 10, 0),
+     [(2, 1, 0, 2, 0.5, 0.5, 0.0), (300, 0, 1, 2, 1.0, 0.0, 0.0)]),
+])
+@pytest.mark.parametrize("fast", [True, False])
+def test_classification_rules(emulator, port, tmp_path, name, variant, cfg, masks, fast):
+    """Shots settled 32 at a time (empty syndromes, weight-1 matches of a
+    one-position first iteration) get the per-shot path's results under every
+    rule that decides whether that iteration is searched: the mode / threshold /
+    cap branches and phase masks whose order for one position lists no weight 1
+    or lists it after another phase.  Errors are supplied, so a match that
+    differs from the supplied error (a stabilizer away) takes the per-shot path
+    for its degeneracy test; fast=False sends every shot there."""
+    code = synth.BB_CODES[72]()
+    errors = np.concatenate([synth.css_shots(code.hz, 70, p, seed=1000 + i)[0]
+                             for i, p in enumerate((0.005, 0.02))])
+    errors[3] = code.hx[0]          # a stabilizer: empty syndrome, nonzero error
+    errors[4] = 0
+    errors[4, 5] = 1
+    errors[4] ^= code.hx[1]         # single-column syndrome, error one stabilizer away
+    phase = synth.write_phase_file(str(tmp_path / "phase.txt"), masks) if masks else None
+    d = tmp_path / "run"
+    d.mkdir()
+    res, dec, log = _run(emulator, str(d), code.hz, code.hx, errors, True, variant, cfg, masks, 12,
+                         fast=fast)
+    prc, pres, pdec = port.css(O.PROB if variant else O.UNIFORM, code.hx, code.hz, errors, None,
+                               O.Config(*cfg), "x", phase)
+    assert prc == 0
+    _compare(res, dec, pres, pdec)
+    if not fast:
+        assert _slow(log) == len(errors), log
+    else:
+        assert _slow(log) < len(errors), log  # empty syndromes at least were settled
+
+
+@pytest.mark.parametrize("fast", [True, False])
+def test_dem_classification(emulator, port, tmp_path, fast):
+    """DEM records with the true logicals in their own array (the C ABI's layout):
+    one-position matches compare the mechanism's logical flips with the truth;
+    cap 0 skips every first iteration (upstream's cap keeps the last accepted
+    set, here none)."""
+    dem = synth.random_dem(12, detectors=40, mechanisms=160, logicals=5, p_range=(2e-3, 1e-2))
+    det, log, _ = synth.dem_shots(dem, 150, seed=44)
+    for cap in (24, 0):
+        cfg = (3, 256, 0, cap, 10, -1)
+        d = tmp_path / f"run{cap}"
+        d.mkdir()
+        res, dec, out, dlog, _ = _run(emulator, str(d), dem.h, None, det, False, 0, cfg, [], 12,
+                                      L=dem.l, logicals=log, fast=fast)
+        prc, pres, pdec, pdlog, _ = port.dem(O.UNIFORM, dem.h, dem.l, det, log, O.Config(*cfg))
+        assert prc == 0
+        _compare(res, dec, pres, pdec)
+        assert np.array_equal(dlog, pdlog)
