@@ -105,6 +105,13 @@ int grand_engine_set_tuning(GrandEngine *engine, int light_log2, int tile_k,
 int grand_engine_kernel_times(GrandEngine *engine, void *stream, float *reset_ms,
                               float *decode_ms);
 
+/* Work statistics of the last device decode on `stream` (after
+ * grand_engine_sync_status): out[0] shots settled by classification (empty
+ * syndromes, one-position weight-1 matches), out[1] shots that took the
+ * per-shot path, out[2] Jobs published, out[3] search tiles of those Jobs,
+ * out[4] scratch words staged for them. */
+int grand_engine_launch_stats(GrandEngine *engine, void *stream, long long *out);
+
 /* Times of the last host-buffer decode (grand_engine_decode / _decode_plain):
  * copies in, the control-word reset(s), the decode kernel(s) and copies out,
  * from CUDA events on the call's stream.  With zero-copy (records read and results

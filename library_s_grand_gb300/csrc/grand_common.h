@@ -66,19 +66,38 @@ enum StatusBits : unsigned {
   kStatusWaitLimit = 1u << 4,     // a bounded wait for another warp gave up (never expected)
 };
 
-// Batch control words (DevBatch::counters, 32 x u64, zeroed before every launch).
+// Batch control block (DevBatch::counters, kCtlBytes zeroed before every launch):
+// each control word sits alone on a 128-byte line (word k at counters[k * kCtrStride]),
+// so that warps polling or drawing from one do not queue behind traffic on another;
+// the status word has the last line.
+constexpr int kCtrStride = 16;           // u64 per line
+constexpr int kCtlBytes = 2048;          // 15 control lines + the status line
+constexpr int kStatusByteOffset = 1920;  // DevBatch::status within the block
+// The workspace's launch epoch (DevBatch::epoch) follows the block on a line of its
+// own and is not zeroed: the last warp of a launch advances it.  Slow-queue
+// entries and Jobs carry the epoch of the launch that wrote them, so a reader can
+// tell an entry written in this launch from one left by an earlier launch without
+// clearing the arrays between launches (they are zeroed once, when allocated).
+constexpr int kCtlAllocBytes = kCtlBytes + 128;
 enum Counter {
-  kCtrJobsReserved = 0,   // (jobs << 40) | tiles, reserved by publishing warps
-  kCtrNextTile = 1,       // next search tile to draw
+  kCtrJobs = 0,           // (Jobs << 40) | tiles reserved, in slot order
+  kCtrFront = 1,          // (Jobs << 40) | tiles of the leading Jobs that are all written
+  kCtrNextTile = 12,      // next search tile to draw (tiles numbered over all Jobs)
   kCtrScratchTop = 2,     // words of the scratch arena in use
   kCtrNextChunk = 3,      // next 32-slot classification chunk to draw
-  kCtrQueuePublished = 4, // slow-queue entries readable (published in reservation order)
-  kCtrQueueHead = 5,      // slow-queue entries drawn
+  kCtrQueueReserved = 4,  // slow-queue entries reserved (each is written right after)
+  kCtrQueueHead = 5,      // slow-queue tickets drawn (a ticket past the reserved
+                          // count is held until its entry exists or the batch ends)
   kCtrChunksDone = 6,     // classification chunks finished
-  kCtrSlowDone = 7,       // slow-path shots finished (their Jobs published)
-  kCtrJobsPublished = 8,  // (jobs << 40) | tiles whose Jobs are fully written
-  kCtrQueueReserved = 9,  // slow-queue entries reserved by appending warps
+  kCtrSlowDone = 7,       // per-shot-path shots finished (their Jobs published)
+  kCtrWarpsDone = 8,      // warps that left the kernel (the last advances the epoch)
+  kCtrSettled = 10,       // shots settled by classification (statistics)
 };
+
+// Address of control word k.
+GRAND_HD inline unsigned long long *ctr_ptr(unsigned long long *counters, int k) {
+  return counters + k * kCtrStride;
+}
 
 // Immutable per-code tables plus the per-call search parameters.
 struct DevCode {
@@ -154,8 +173,9 @@ struct alignas(128) Job {
   int nseg;
   int final_iteration, final_tam; // outcome fields if nothing is found
   int it_lo;                      // first iteration searched by the search kernel
-  unsigned long long tile_base;   // first global tile
+  unsigned long long tile_base;   // first tile of the Job (tiles numbered over all Jobs)
   unsigned long long ntiles;
+  unsigned ready;                 // launch tag (epoch + 1) once the Job is fully written
   unsigned long long best;        // lowest matching global index (atomicMin)
   unsigned long long tiles_done;
   int original_weight;
@@ -194,7 +214,9 @@ struct DevBatch {
   unsigned long long scratch_words;
   unsigned *status;
   int *deferred;                 // per shot: 1 if the shot must be re-run
-  int *queue;                    // num_shots slots: launch slots that need the per-shot path
+  unsigned long long *queue;     // num_shots entries: ((epoch + 1) << 32) | launch slot of a
+                                 // shot that needs the per-shot path
+  unsigned *epoch;               // the workspace's launch epoch (kCtlAllocBytes layout)
   int fast;                      // 1: settle shots 32 at a time first (empty syndromes, and
                                  //    weight-1 matches of a one-position first iteration)
   int light_max_log2;            // light-path budget (candidates, log2)

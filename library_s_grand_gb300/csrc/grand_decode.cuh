@@ -14,16 +14,19 @@
 // warps are still classifying and triaging, and triage and search share the GPU
 // instead of running as two launches one after the other.
 //
-// Drawing: chunks by atomicAdd (a draw past the end is dropped), queue entries
-// by compare-and-swap below the published count, tiles by atomicAdd below the
-// published tile total -- a tile drawn past it stays with the warp (held) until
-// a Job covering it is published or the batch has no more work.  Queue entries
-// and Jobs are published in reservation order, each once it is fully written.
+// Drawing: chunks by atomicAdd (a draw past the end is dropped); slow-queue
+// entries by atomicAdd tickets -- a ticket past the reserved count stays with the
+// warp until its entry is reserved or the batch has no more -- and each entry is
+// read once it carries this launch's tag; search tiles by atomicAdd below the
+// tiles of the front -- the leading Jobs all marked ready with the tag, which
+// any warp advances past a ready Job -- a tile drawn past it stays with the warp
+// until a Job covering it is written.  One atomic per draw, whatever the number
+// of waiting warps, and no warp waits for another to publish in order.
 //
 // A warp that finds nothing to do sleeps and polls (bounded, kStatusWaitLimit on
 // exhaustion).  It waits only for work that running warps are producing -- they
 // never wait for it -- and leaves once every chunk and slow shot is finished and
-// no published tile is left undrawn.
+// every Job's tiles are drawn.  The last warp to leave advances the launch epoch.
 #pragma once
 
 #include "grand_search.cuh"
@@ -32,27 +35,6 @@
 namespace grand {
 
 constexpr int kDecodeMinBlocks = 4;  // resident blocks per SM the register budget allows
-
-__device__ __forceinline__ unsigned long long ld_ctr(const DevBatch &b, int ctr) {
-  return *reinterpret_cast<volatile unsigned long long *>(b.counters + ctr);
-}
-
-// Lane 0: the next slow-queue entry below the published count (-1 if none now).
-__device__ __forceinline__ int draw_slow(const DevBatch &b) {
-  unsigned long long h = ld_ctr(b, kCtrQueueHead);
-  for (int guard = 0; guard < 64; ++guard) {
-    const unsigned long long avail = b.fast ? ld_ctr(b, kCtrQueuePublished)
-                                            : (unsigned long long)b.num_shots;
-    if (h >= avail) return -1;
-    const unsigned long long seen = atomicCAS(&b.counters[kCtrQueueHead], h, h + 1ull);
-    if (seen == h) {
-      if (!b.fast) return (int)h;  // every slot takes the per-shot path
-      return *reinterpret_cast<volatile int *>(b.queue + h);
-    }
-    h = seen;
-  }
-  return -1;
-}
 
 // What a warp does next (decided by lane 0 from the control words, then
 // broadcast, so that the whole warp takes the same path).
@@ -67,9 +49,14 @@ __global__ void __launch_bounds__(kDecodeWarps * 32, kDecodeMinBlocks) decode_ke
   WarpArea &A = areas[wib];
   SearchCache cache;
   cache.reset();
+  // this launch's tag: entries and Jobs written now carry epoch + 1 (the epoch
+  // changes only once every warp of the launch has left)
+  const unsigned epoch = *reinterpret_cast<volatile unsigned *>(b.epoch);
+  const unsigned tag = epoch + 1u;
   const unsigned long long nchunks = b.fast ? (unsigned long long)((b.num_shots + 31) / 32) : 0ull;
   const unsigned long long nwarps = (unsigned long long)gridDim.x * kDecodeWarps;
   constexpr unsigned long long kTileMask = (1ull << 40) - 1ull;
+  unsigned long long ticket = kNone;            // lane 0: a slow-queue ticket not yet used
   unsigned long long held_lo = 0, held_hi = 0;  // lane 0: tiles drawn and not yet run
   int polls = 0;
   for (;;) {
@@ -78,7 +65,7 @@ __global__ void __launch_bounds__(kDecodeWarps * 32, kDecodeMinBlocks) decode_ke
     if (lane == 0) {
       // 1. classification chunks (a draw past the end is dropped)
       if (nchunks && ld_ctr(b, kCtrNextChunk) < nchunks) {
-        const unsigned long long k = atomicAdd(&b.counters[kCtrNextChunk], 1ull);
+        const unsigned long long k = atomicAdd(ctr_ptr(b.counters, kCtrNextChunk), 1ull);
         if (k < nchunks) {
           step = kStepChunk;
           a0 = k;
@@ -86,24 +73,46 @@ __global__ void __launch_bounds__(kDecodeWarps * 32, kDecodeMinBlocks) decode_ke
       }
       // 2. the per-shot path
       if (step == kStepWait) {
-        const int slot = draw_slow(b);
-        if (slot >= 0) {
-          step = kStepShot;
-          a0 = (unsigned long long)slot;
+        const unsigned long long reserved =
+            b.fast ? ld_ctr(b, kCtrQueueReserved) : (unsigned long long)b.num_shots;
+        if (ticket == kNone && ld_ctr(b, kCtrQueueHead) < reserved)
+          ticket = atomicAdd(ctr_ptr(b.counters, kCtrQueueHead), 1ull);
+        if (ticket != kNone && ticket < reserved) {
+          if (!b.fast) {
+            step = kStepShot;
+            a0 = ticket;
+          } else {
+            // the appending warp writes the entry right after reserving it
+            volatile unsigned long long *e = b.queue + ticket;
+            unsigned long long v = *e;
+            for (int p = 0; (unsigned)(v >> 32) != tag; ++p) {
+              if (p >= kShortPolls) break;
+              nap(p);
+              v = *e;
+            }
+            if ((unsigned)(v >> 32) == tag) {
+              step = kStepShot;
+              a0 = v & 0xffffffffull;
+            } else {
+              atomicOr(b.status, kStatusWaitLimit);
+            }
+          }
+          ticket = kNone;
         }
       }
-      // 3. search tiles.  Several tiles per draw when many are left (the
-      // lookups are then paid once per draw), one at a time when few are, so
-      // that a handful of expensive Jobs still spreads over every warp.
+      // 3. search tiles of the Jobs before the front.  Several tiles per draw
+      // when many are left (the lookups are then paid once per draw), one at a
+      // time when few are, so that a handful of expensive Jobs still spreads
+      // over every warp; a draw past the front's tiles is held until they exist.
       if (step == kStepWait) {
-        const unsigned long long pub = ld_ctr(b, kCtrJobsPublished);
-        const unsigned long long njobs = pub >> 40, ptiles = pub & kTileMask;
+        const unsigned long long front = ld_ctr(b, kCtrFront);
+        const unsigned long long njobs = front >> 40, ptiles = front & kTileMask;
         if (held_lo >= held_hi) {
           const unsigned long long next = ld_ctr(b, kCtrNextTile);
           if (next < ptiles) {
             unsigned long long f = kTilesPerFetch;
             while (f > 1ull && ptiles - next < 8ull * f * nwarps) f >>= 1;
-            held_lo = atomicAdd(&b.counters[kCtrNextTile], f);
+            held_lo = atomicAdd(ctr_ptr(b.counters, kCtrNextTile), f);
             held_hi = held_lo + f;
           }
         }
@@ -118,14 +127,23 @@ __global__ void __launch_bounds__(kDecodeWarps * 32, kDecodeMinBlocks) decode_ke
       // 4. done, or wait for the warps still producing work
       if (step == kStepWait && ld_ctr(b, kCtrChunksDone) >= nchunks) {
         __threadfence();
-        const unsigned long long queued =
-            b.fast ? ld_ctr(b, kCtrQueuePublished) : (unsigned long long)b.num_shots;
-        if (ld_ctr(b, kCtrQueueHead) >= queued && ld_ctr(b, kCtrSlowDone) >= queued) {
-          // every Job is published: tiles past the total will never exist
+        const unsigned long long reserved =
+            b.fast ? ld_ctr(b, kCtrQueueReserved) : (unsigned long long)b.num_shots;
+        if (ld_ctr(b, kCtrSlowDone) >= reserved) {
+          // every slow shot is done and its Job written (a ticket past the
+          // entries will never be filled); once the front has passed every Job,
+          // tiles past its total will never exist
+          ticket = kNone;
           __threadfence();
-          const unsigned long long total = ld_ctr(b, kCtrJobsPublished) & kTileMask;
-          if (held_lo >= total) held_lo = held_hi = 0;
-          if (held_lo >= held_hi && ld_ctr(b, kCtrNextTile) >= total) step = kStepExit;
+          const unsigned long long front = ld_ctr(b, kCtrFront);
+          if ((front >> 40) >= (ld_ctr(b, kCtrJobs) >> 40) ||
+              (front >> 40) >= (unsigned long long)b.max_jobs) {
+            const unsigned long long total = front & kTileMask;
+            if (held_lo >= total) held_lo = held_hi = 0;
+            if (held_lo >= held_hi && ld_ctr(b, kCtrNextTile) >= total) step = kStepExit;
+          } else {
+            advance_front(b, tag);  // a publisher's advance can lose a race: help it
+          }
         }
       }
     }
@@ -142,24 +160,31 @@ __global__ void __launch_bounds__(kDecodeWarps * 32, kDecodeMinBlocks) decode_ke
     polls = 0;
     a0 = __shfl_sync(kFull, a0, 0);
     if (step == kStepChunk) {
-      classify_chunk<MLK>(b, (int)a0, A);
+      classify_chunk<MLK>(b, (int)a0, A, tag);
       cache.stage_lost();
       if (lane == 0) {
         __threadfence();
-        atomicAdd(&b.counters[kCtrChunksDone], 1ull);
+        atomicAdd(ctr_ptr(b.counters, kCtrChunksDone), 1ull);
       }
     } else if (step == kStepShot) {
-      triage_shot<MLK>(b, (int)a0, A, plans[wib]);
+      triage_shot<MLK>(b, (int)a0, A, plans[wib], tag);
       cache.stage_lost();
       if (lane == 0) {
         __threadfence();
-        atomicAdd(&b.counters[kCtrSlowDone], 1ull);
+        atomicAdd(ctr_ptr(b.counters, kCtrSlowDone), 1ull);
       }
     } else {
       a1 = __shfl_sync(kFull, a1, 0);
       a2 = __shfl_sync(kFull, a2, 0);
       search_tiles<MLK>(b, a0, a1, a2, A, cache);
     }
+  }
+  // the last warp to leave advances the epoch for the next launch
+  __syncwarp();
+  if (lane == 0) {
+    __threadfence();
+    if (atomicAdd(ctr_ptr(b.counters, kCtrWarpsDone), 1ull) + 1ull == nwarps)
+      *reinterpret_cast<volatile unsigned *>(b.epoch) = tag;
   }
 }
 

@@ -238,11 +238,11 @@ int grand_engine_decode_device(GrandEngine *e, int num_shots, const int *d_shot_
   }
   const int max_jobs = num_shots;
   const size_t scratch_words = 64ull << 20;
-  cudaError_t r = ensure(&slot->d_jobs, &slot->cap_jobs, sizeof(Job) * (size_t)max_jobs);
+  cudaError_t r = ensure_zeroed(&slot->d_jobs, &slot->cap_jobs, sizeof(Job) * (size_t)max_jobs);
   if (r == cudaSuccess) r = ensure(&slot->d_scratch, &slot->cap_scratch, scratch_words * 4);
-  if (r == cudaSuccess) r = ensure(&slot->d_small, &slot->cap_small, 256);
+  if (r == cudaSuccess) r = ensure_zeroed(&slot->d_small, &slot->cap_small, kCtlAllocBytes);
   if (r == cudaSuccess)
-    r = ensure(&slot->d_deferred, &slot->cap_deferred, 2 * sizeof(int) * (size_t)num_shots);
+    r = ensure_zeroed(&slot->d_deferred, &slot->cap_deferred, shot_buffer_bytes(num_shots));
   if (r != cudaSuccess) {
     set_error("grand: device workspace allocation failed (%s)", cudaGetErrorString(r));
     return GRAND_ERR_CUDA;
@@ -260,11 +260,12 @@ int grand_engine_decode_device(GrandEngine *e, int num_shots, const int *d_shot_
   b.jobs = (Job *)slot->d_jobs;
   b.max_jobs = max_jobs;
   b.counters = (unsigned long long *)slot->d_small;
-  b.status = (unsigned *)((char *)slot->d_small + 128);
+  b.status = (unsigned *)((char *)slot->d_small + kStatusByteOffset);
   b.scratch = (uint32_t *)slot->d_scratch;
   b.scratch_words = scratch_words;
   b.deferred = (int *)slot->d_deferred;
-  b.queue = (int *)slot->d_deferred + num_shots;
+  b.queue = shot_queue(slot->d_deferred, num_shots);
+  b.epoch = (unsigned *)((char *)slot->d_small + kCtlBytes);
   b.fast = e->tn.fast;
   b.light_max_log2 = e->tn.light_max_log2;
   b.tile_k = e->tn.tile_k;
@@ -319,7 +320,8 @@ int grand_engine_sync_status(GrandEngine *e, void *stream) {
     std::lock_guard<std::mutex> lk(e->mu);
     auto it = e->slots.find(stream);
     if (it == e->slots.end()) return 0;
-    r = cudaMemcpy(&st, (char *)it->second->d_small + 128, sizeof(unsigned), cudaMemcpyDeviceToHost);
+    r = cudaMemcpy(&st, (char *)it->second->d_small + kStatusByteOffset, sizeof(unsigned),
+                   cudaMemcpyDeviceToHost);
   }
   if (r != cudaSuccess) return GRAND_ERR_CUDA;
   if (st & (kStatusJobOverflow | kStatusScratchOverflow)) {
@@ -331,6 +333,22 @@ int grand_engine_sync_status(GrandEngine *e, void *stream) {
     return GRAND_ERR_LIMIT;
   }
   if (st & kStatusCasLimit) return GRAND_ERR_CUDA;
+  return 0;
+}
+
+int grand_engine_launch_stats(GrandEngine *e, void *stream, long long *out) {
+  if (!e || !out) return GRAND_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(e->mu);
+  auto it = e->slots.find(stream);
+  if (it == e->slots.end()) return GRAND_ERR_INVALID;
+  std::vector<unsigned long long> c(kCtlBytes / 8);
+  if (cudaMemcpy(c.data(), it->second->d_small, kCtlBytes, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return GRAND_ERR_CUDA;
+  out[0] = (long long)c[kCtrSettled * kCtrStride];
+  out[1] = (long long)c[kCtrSlowDone * kCtrStride];
+  out[2] = (long long)(c[kCtrJobs * kCtrStride] >> 40);
+  out[3] = (long long)(c[kCtrJobs * kCtrStride] & ((1ull << 40) - 1ull));
+  out[4] = (long long)c[kCtrScratchTop * kCtrStride];
   return 0;
 }
 

@@ -58,6 +58,13 @@ cudaError_t ensure(void **p, size_t *cap, size_t bytes) {
   return e;
 }
 
+cudaError_t ensure_zeroed(void **p, size_t *cap, size_t bytes) {
+  void *before = *p;
+  cudaError_t e = ensure(p, cap, bytes);
+  if (e == cudaSuccess && *p != before) e = cudaMemset(*p, 0, *cap);
+  return e;
+}
+
 CodeTables::~CodeTables() {
   cudaFree(cols);
   cudaFree(colw);
@@ -380,7 +387,7 @@ int decode_blocks_per_sm(int occupancy_bps, const Tuning &tn) {
 
 cudaError_t launch_pipeline(const Context *ctx, const DevBatch &b, const Tuning &tn,
                             cudaStream_t s, cudaEvent_t mid) {
-  cudaError_t e = cudaMemsetAsync(b.counters, 0, 256, s);
+  cudaError_t e = cudaMemsetAsync(b.counters, 0, kCtlBytes, s);
   if (e != cudaSuccess) return e;
   if (mid) cudaEventRecord(mid, s);
   // persistent: as many blocks as are resident at once (fewer for a small batch,
@@ -411,12 +418,12 @@ int run_batch(Context *ctx, Workspace *ws, const BatchRequest &req, BatchTiming 
     if (req.h_cost) CK(ensure(&ws->d_cost, &ws->cap_cost, sizeof(float) * N));
   }
   const int max_jobs = std::min(N, 16384);
-  CK(ensure(&ws->d_jobs, &ws->cap_jobs, sizeof(Job) * max_jobs));
+  CK(ensure_zeroed(&ws->d_jobs, &ws->cap_jobs, sizeof(Job) * max_jobs));
   const size_t scratch_words = 32ull << 20;
   CK(ensure(&ws->d_scratch, &ws->cap_scratch, scratch_words * 4));
-  size_t small_cap = ws->d_small ? 256 : 0;
-  CK(ensure(&ws->d_small, &small_cap, 256));
-  CK(ensure(&ws->d_deferred, &ws->cap_deferred, 2 * sizeof(int) * N));
+  size_t small_cap = ws->d_small ? kCtlAllocBytes : 0;
+  CK(ensure_zeroed(&ws->d_small, &small_cap, kCtlAllocBytes));
+  CK(ensure_zeroed(&ws->d_deferred, &ws->cap_deferred, shot_buffer_bytes(N)));
 
   // Per-call host work is kept to the launches, one status read and one
   // synchronisation; events are recorded only when the caller asks for times,
@@ -483,11 +490,12 @@ int run_batch(Context *ctx, Workspace *ws, const BatchRequest &req, BatchTiming 
   b.jobs = (Job *)ws->d_jobs;
   b.max_jobs = max_jobs;
   b.counters = (unsigned long long *)ws->d_small;
-  b.status = (unsigned *)((char *)ws->d_small + 128);
+  b.status = (unsigned *)((char *)ws->d_small + kStatusByteOffset);
   b.scratch = (uint32_t *)ws->d_scratch;
   b.scratch_words = scratch_words;
   b.deferred = (int *)ws->d_deferred;
-  b.queue = (int *)ws->d_deferred + N;
+  b.queue = shot_queue(ws->d_deferred, N);
+  b.epoch = (unsigned *)((char *)ws->d_small + kCtlBytes);
   b.fast = tn.fast;
   b.light_max_log2 = tn.light_max_log2;
   b.tile_k = tn.tile_k;

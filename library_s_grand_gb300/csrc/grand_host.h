@@ -71,7 +71,7 @@ struct Workspace {
   void *d_jobs = nullptr; size_t cap_jobs = 0;
   void *d_scratch = nullptr; size_t cap_scratch = 0;
   void *d_small = nullptr;  // counters, status
-  void *d_deferred = nullptr; size_t cap_deferred = 0;  // 2 x shots: flags, then the slow queue
+  void *d_deferred = nullptr; size_t cap_deferred = 0;  // shot_buffer_bytes: flags, slow queue
   void *d_map = nullptr; size_t cap_map = 0;
   void *d_codes = nullptr; size_t cap_codes = 0;
   void *h_codes = nullptr; size_t cap_hcodes = 0;  // pinned staging of the DevCode array
@@ -84,6 +84,19 @@ struct Workspace {
 };
 
 cudaError_t ensure(void **p, size_t *cap, size_t bytes);
+// As ensure, and a new allocation starts zeroed (buffers whose entries carry a
+// launch tag: zero is no launch's tag).
+cudaError_t ensure_zeroed(void **p, size_t *cap, size_t bytes);
+
+// Bytes of the per-shot buffer: num_shots re-run flags (int), then, 8-byte
+// aligned, num_shots slow-queue entries (u64).
+inline size_t shot_buffer_bytes(size_t num_shots) {
+  return ((4 * num_shots + 7) & ~(size_t)7) + 8 * num_shots;
+}
+inline unsigned long long *shot_queue(void *shot_buffer, size_t num_shots) {
+  return reinterpret_cast<unsigned long long *>(static_cast<char *>(shot_buffer) +
+                                                ((4 * num_shots + 7) & ~(size_t)7));
+}
 
 class Context {
  public:

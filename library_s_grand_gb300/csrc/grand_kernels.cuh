@@ -45,35 +45,39 @@ struct PlanState {
 // Bounded waits.  A warp that waits for another warp's progress sleeps between
 // polls, longer as the wait goes on; after kWaitPolls polls it gives up and
 // raises kStatusWaitLimit (never expected: every wait is for a warp that is
-// running and waits for nothing this warp holds).
+// running and waits for nothing this warp holds).  kShortPolls bounds the
+// waits for an entry or Job another warp has reserved and is writing.
 constexpr int kWaitPolls = 1 << 21;
+constexpr int kShortPolls = 1 << 16;
 
 __device__ __forceinline__ void nap(int polls) {
 #ifdef GRAND_HOST_EMULATION
   grand_host_nap(polls);
 #else
-  __nanosleep(polls < 8 ? 32u : (polls < 64 ? 256u : 1000u));
+  __nanosleep(polls < 4 ? 200u : (polls < 32 ? 800u : 2000u));
 #endif
 }
 
-// Lane 0 only.  Counter `ctr` is advanced in reservation order: once it holds
-// `mine` (every earlier reservation published) this warp sets it to `next`.  The
-// fence orders the warp's writes (made visible to lane 0 by the caller's
-// __syncwarp after each lane fenced its own) before the counter.
-__device__ __forceinline__ void publish_in_order(const DevBatch &b, int ctr,
-                                                 unsigned long long mine,
-                                                 unsigned long long next) {
-  __threadfence();
-  volatile unsigned long long *c = b.counters + ctr;
-  for (int polls = 0; *c != mine; ++polls) {
-    if (polls >= kWaitPolls) {
-      atomicOr(b.status, kStatusWaitLimit);
-      break;
-    }
-    nap(polls);
+__device__ __forceinline__ unsigned long long ld_ctr(const DevBatch &b, int ctr) {
+  return *reinterpret_cast<volatile unsigned long long *>(ctr_ptr(b.counters, ctr));
+}
+
+// Lane 0.  Jobs are searchable from the front: the leading Jobs whose ready words
+// carry this launch's tag.  Whoever finds the Job at the front written moves the
+// front past it (and on, while the next is written too).  A publisher calls this
+// after marking its Job ready, so every written Job is passed: the publisher of
+// the last Job to become ready finds all before it written.
+__device__ __forceinline__ void advance_front(const DevBatch &b, unsigned tag) {
+  unsigned long long f = ld_ctr(b, kCtrFront);
+  for (int guard = 0; guard < (1 << 20); ++guard) {
+    const unsigned long long j = f >> 40;
+    if (j >= (ld_ctr(b, kCtrJobs) >> 40) || j >= (unsigned long long)b.max_jobs) return;
+    const Job *J = b.jobs + j;
+    if (*reinterpret_cast<const volatile unsigned *>(&J->ready) != tag) return;
+    const unsigned long long nt = *reinterpret_cast<const volatile unsigned long long *>(&J->ntiles);
+    const unsigned long long seen = atomicCAS(ctr_ptr(b.counters, kCtrFront), f, f + (1ull << 40) + nt);
+    f = seen == f ? f + (1ull << 40) + nt : seen;
   }
-  *c = next;
-  __threadfence();
 }
 
 // ---------------------------------------------------------------------------

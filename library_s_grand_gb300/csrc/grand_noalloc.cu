@@ -35,19 +35,20 @@ constexpr size_t kOffCode = align256(kOffNcr + sizeof(unsigned long long) * (kMa
 constexpr size_t kOffCols = align256(kOffCode + sizeof(DevCode));
 constexpr size_t kOffColw = align256(kOffCols + sizeof(uint32_t) * kNaMaxCols * 8);
 constexpr size_t kOffHcol = align256(kOffColw + sizeof(int) * kNaMaxCols);
-constexpr size_t kOffSmall = align256(kOffHcol + sizeof(uint32_t) * kNaMaxCols);  // counters, +128: status
-constexpr size_t kOffDeferred = align256(kOffSmall + 256);
+constexpr size_t kOffSmall = align256(kOffHcol + sizeof(uint32_t) * kNaMaxCols);  // control block
+constexpr size_t kOffDeferred = align256(kOffSmall + kCtlAllocBytes);
 constexpr size_t kOffMap = align256(kOffDeferred + sizeof(int) * kNaChunk);     // re-run list
 constexpr size_t kOffMapCount = align256(kOffMap + sizeof(int) * kNaChunk);     // its length
 constexpr size_t kOffQueue = align256(kOffMapCount + 256);                       // slow queue
-constexpr size_t kOffJobs = align256(kOffQueue + sizeof(int) * kNaChunk);
+constexpr size_t kOffJobs = align256(kOffQueue + sizeof(unsigned long long) * kNaChunk);
 constexpr size_t kOffArena = align256(kOffJobs + sizeof(Job) * kNaChunk);
 constexpr size_t kScratchBytes = align256(kOffArena + sizeof(uint32_t) * kNaArenaWords);
 
 }  // namespace
 
 // All no-allocation calls on a device share this array; it exists for the life
-// of the process on every device that loads this part of the library.
+// of the process on every device that loads this part of the library.  It starts
+// zeroed, as the launch tags of its queue entries and Jobs require.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
 namespace {
@@ -244,8 +245,6 @@ extern "C" int grand_decode_cc_noalloc(const int *d_H, int n, int m, const int *
   noalloc_pack_kernel<<<(m + 127) / 128, 128, 0, s>>>(d_H, n, m, nwp, cols, colw, hcol);
   noalloc_code_kernel<<<1, 256, 0, s>>>(t, colw, m, code);
   e = cudaGetLastError();
-  // the status word starts at zero for every call; it then collects all chunks
-  if (e == cudaSuccess) e = cudaMemsetAsync(base + kOffSmall + 128, 0, 128, s);
 
   const Tuning &tn = tuning();
   // the decode kernel's CTAs per SM as the regular entry points choose them
@@ -266,11 +265,12 @@ extern "C" int grand_decode_cc_noalloc(const int *d_H, int n, int m, const int *
     b.jobs = reinterpret_cast<Job *>(base + kOffJobs);
     b.max_jobs = kNaChunk;
     b.counters = reinterpret_cast<unsigned long long *>(base + kOffSmall);
-    b.status = reinterpret_cast<unsigned *>(base + kOffSmall + 128);
+    b.status = reinterpret_cast<unsigned *>(base + kOffSmall + kStatusByteOffset);
     b.scratch = reinterpret_cast<uint32_t *>(base + kOffArena);
     b.scratch_words = kNaArenaWords;
     b.deferred = reinterpret_cast<int *>(base + kOffDeferred);
-    b.queue = reinterpret_cast<int *>(base + kOffQueue);
+    b.queue = reinterpret_cast<unsigned long long *>(base + kOffQueue);
+    b.epoch = reinterpret_cast<unsigned *>(base + kOffSmall + kCtlBytes);
     b.fast = tn.fast;
     b.light_max_log2 = tn.light_max_log2;
     b.tile_k = tn.tile_k;
@@ -283,11 +283,12 @@ extern "C" int grand_decode_cc_noalloc(const int *d_H, int n, int m, const int *
       b.num_shots = todo;
       b.shot_map = round == 0 ? nullptr : map;
       // control words and status restart for every round
-      e = cudaMemsetAsync(base + kOffSmall, 0, 256, s);
+      e = cudaMemsetAsync(base + kOffSmall, 0, kCtlBytes, s);
       if (e == cudaSuccess) e = launch_decode(b, g_sms[dev] * per_sm, s);
       unsigned rs = 0;
       if (e == cudaSuccess)
-        e = cudaMemcpyAsync(&rs, base + kOffSmall + 128, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+        e = cudaMemcpyAsync(&rs, base + kOffSmall + kStatusByteOffset, sizeof(unsigned),
+                            cudaMemcpyDeviceToHost, s);
       if (e == cudaSuccess) e = cudaStreamSynchronize(s);
       if (e != cudaSuccess) break;
       st |= rs & ~(unsigned)(kStatusScratchOverflow | kStatusJobOverflow);

@@ -95,9 +95,9 @@ struct SearchCache {
   __device__ void stage_lost() { st_job = st_it = -1; }
 };
 
-// Search tiles [t0, t1) of the launch's published Jobs (njobs of them; every
-// tile below the published total belongs to one of those).  The warp's
-// WarpArea holds the staged sketches (or, while a Job is finished, the Job).
+// Search tiles [t0, t1) of the written Jobs (njobs of them, from slot 0; every
+// tile below their total belongs to one).  The warp's WarpArea holds the staged
+// sketches (or, while a Job is finished, the Job).
 template <bool MLK>
 __device__ void search_tiles(const DevBatch &b, unsigned long long t0, unsigned long long t1,
                              unsigned long long njobs, WarpArea &A, SearchCache &c) {
@@ -212,7 +212,7 @@ __device__ void search_tiles(const DevBatch &b, unsigned long long t0, unsigned 
           atomicOr(b.status, kStatusCasLimit);
       }
     }
-    // tiles of this range done for the current job: posted once per job per range
+    // tiles of this range done for the current Job: posted once per Job per range
     pending += 1ull;
     fenced = fenced || published;
     const bool flush = (t + 1 == t1) || (t + 1 >= c.cj_hi);

@@ -144,11 +144,12 @@ cudaError_t start_slot(GrandServer *S, SrvSlot *sl) {
   b.jobs = sl->d_jobs;
   b.max_jobs = S->max_shots;
   b.counters = sl->d_small;
-  b.status = (unsigned *)((char *)sl->d_small + 128);
+  b.status = (unsigned *)((char *)sl->d_small + kStatusByteOffset);
   b.scratch = sl->d_scratch;
   b.scratch_words = kSrvArenaWords;
   b.deferred = sl->d_deferred;
-  b.queue = sl->d_deferred + S->max_shots;
+  b.queue = shot_queue(sl->d_deferred, S->max_shots);
+  b.epoch = (unsigned *)((char *)sl->d_small + kCtlBytes);
   b.fast = e->tn.fast;
   b.light_max_log2 = e->tn.light_max_log2;
   b.tile_k = e->tn.tile_k;
@@ -276,8 +277,8 @@ int grand_server_create(GrandEngine *e, int slots, int max_shots, size_t budget,
   const size_t resb = align256(sizeof(GrandDecoderResult) * max_shots);
   const size_t jobb = align256(sizeof(Job) * max_shots);
   const size_t arena = align256(sizeof(uint32_t) * kSrvArenaWords);
-  const size_t smallb = 256;
-  const size_t defb = align256(2 * sizeof(int) * max_shots);  // re-run flags, then the slow queue
+  const size_t smallb = align256(kCtlAllocBytes);
+  const size_t defb = align256(shot_buffer_bytes(max_shots));  // re-run flags, then the slow queue
   const size_t per_slot = rec + offb + codeb + resb + jobb + arena + smallb + defb;
   size_t free_b = 0, total_b = 0;
   if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
@@ -299,6 +300,7 @@ int grand_server_create(GrandEngine *e, int slots, int max_shots, size_t budget,
     const size_t hb = rec + offb + codeb + resb + 256;
     if (err == cudaSuccess) err = cudaHostAlloc(&sl->h_block, hb, cudaHostAllocDefault);
     if (err == cudaSuccess) err = cudaMalloc(&sl->d_block, per_slot);
+    if (err == cudaSuccess) err = cudaMemset(sl->d_block, 0, per_slot);  // no launch's tags
     if (err != cudaSuccess) {
       free_slot(sl);
       break;

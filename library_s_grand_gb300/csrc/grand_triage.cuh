@@ -478,9 +478,10 @@ __device__ void light_search(const DevBatch &b, const DevCode &cd, Job &J, WarpA
   }
 }
 
-// The full per-shot path: one warp, launch slot `slot`.  P is the warp's planner state.
+// The full per-shot path: one warp, launch slot `slot`.  P is the warp's planner
+// state; tag (the launch epoch + 1) marks a published Job.
 template <bool MLK>
-__device__ void triage_shot(const DevBatch &b, int slot, WarpArea &A, PlanState &P) {
+__device__ void triage_shot(const DevBatch &b, int slot, WarpArea &A, PlanState &P, unsigned tag) {
   const int lane = threadIdx.x & 31;
   {
     const unsigned long long t_start = global_ns();
@@ -726,9 +727,9 @@ __device__ void triage_shot(const DevBatch &b, int slot, WarpArea &A, PlanState 
       // A reservation that does not fit takes nothing, so one oversized shot
       // does not make the shots after it fail too (they are re-run otherwise).
       ok = 0;
-      off = *reinterpret_cast<volatile unsigned long long *>(&b.counters[2]);
+      off = *reinterpret_cast<volatile unsigned long long *>(ctr_ptr(b.counters, kCtrScratchTop));
       for (int guard = 0; guard < (1 << 16) && off + words <= b.scratch_words; ++guard) {
-        const unsigned long long seen = atomicCAS(&b.counters[2], off, off + words);
+        const unsigned long long seen = atomicCAS(ctr_ptr(b.counters, kCtrScratchTop), off, off + words);
         if (seen == off) {
           ok = 1;
           break;
@@ -811,15 +812,13 @@ __device__ void triage_shot(const DevBatch &b, int slot, WarpArea &A, PlanState 
         S.tile_lo = ntl;
         ntl += S.njt;
       }
-      // Reserve a job slot and the next ntl tiles (job table permitting); a
+      // A Job slot and the next ntl tiles (the job table permitting); a
       // reservation that does not fit takes nothing.
       ok = 0;
-      unsigned long long old =
-          *reinterpret_cast<volatile unsigned long long *>(&b.counters[kCtrJobsReserved]);
+      unsigned long long old = ld_ctr(b, kCtrJobs);
       for (int guard = 0; guard < (1 << 16) && (old >> 40) < (unsigned long long)b.max_jobs;
            ++guard) {
-        const unsigned long long seen =
-            atomicCAS(&b.counters[kCtrJobsReserved], old, old + (1ull << 40) + ntl);
+        const unsigned long long seen = atomicCAS(ctr_ptr(b.counters, kCtrJobs), old, old + (1ull << 40) + ntl);
         if (seen == old) {
           ok = 1;
           break;
@@ -845,6 +844,7 @@ __device__ void triage_shot(const DevBatch &b, int slot, WarpArea &A, PlanState 
       J.ebits = sp;
       J.tile_base = tbase;
       J.ntiles = ntl;
+      J.ready = 0;
       for (int i = 0; i < kMaxIters; ++i)
         for (int w = 0; w <= kMaxW; ++w) J.mlkey[i][w][0] = J.mlkey[i][w][1] = kNone;
     }
@@ -855,15 +855,19 @@ __device__ void triage_shot(const DevBatch &b, int slot, WarpArea &A, PlanState 
       for (int i = lane; i < (int)(sizeof(Job) / 4); i += 32) dst[i] = src[i];
     }
     if (lane == 0 && b.deferred) b.deferred[shot] = 0;
+    // The Job is searchable once its ready word holds this launch's tag: each
+    // lane orders its part of the copy (and the staged scratch) before it.
+    __threadfence();
     __syncwarp();
-    // Jobs become visible to the searching warps in reservation order, each only
-    // once it is fully written: wait for the Jobs reserved before this one.
-    if (lane == 0)
-      publish_in_order(b, kCtrJobsPublished, (jslot << 40) | tbase, ((jslot + 1ull) << 40) | (tbase + ntl));
+    if (lane == 0) {
+      __threadfence();
+      *reinterpret_cast<volatile unsigned *>(&b.jobs[jslot].ready) = tag;
+      __threadfence();
+      advance_front(b, tag);
+    }
     __syncwarp();
   }
 }
-
 
 // ---------------------------------------------------------------------------
 // Classification of 32 launch slots, one lane per shot.
@@ -945,9 +949,10 @@ __device__ __forceinline__ bool one_position_searched(const DevCode &cd, bool *g
 // 0/1 matrices regular or not), found through the columns grouped by their
 // lowest row.  Shots the lanes cannot settle here (ML codes, supplied errors
 // that differ from the match, wide codes, records that are not back to back)
-// take the slow path.
+// take the slow path: they are appended to the slow queue with tag (the launch
+// epoch + 1).
 template <bool MLK>
-__device__ void classify_chunk(const DevBatch &b, int chunk, WarpArea &A) {
+__device__ void classify_chunk(const DevBatch &b, int chunk, WarpArea &A, unsigned tag) {
   FastArea &F = *reinterpret_cast<FastArea *>(&A);
   const int lane = threadIdx.x & 31;
   const unsigned lt_mask = (1u << lane) - 1u;
@@ -1169,6 +1174,8 @@ __device__ void classify_chunk(const DevBatch &b, int chunk, WarpArea &A) {
   }
   __syncwarp();
   const unsigned settled = __ballot_sync(kFull, done);
+  if (lane == 0 && settled)
+    atomicAdd(ctr_ptr(b.counters, kCtrSettled), (unsigned long long)__popc(settled));
   for (unsigned mm = settled; mm; mm &= mm - 1u) {
     const int j = __ffs(mm) - 1;
     const int sj = __shfl_sync(kFull, shot, j);
@@ -1192,12 +1199,13 @@ __device__ void classify_chunk(const DevBatch &b, int chunk, WarpArea &A) {
   const unsigned sm = __ballot_sync(kFull, slow);
   if (sm) {
     unsigned long long base = 0;
-    if (lane == 0) base = atomicAdd(&b.counters[kCtrQueueReserved], (unsigned long long)__popc(sm));
+    if (lane == 0) base = atomicAdd(ctr_ptr(b.counters, kCtrQueueReserved), (unsigned long long)__popc(sm));
     base = __shfl_sync(kFull, base, 0);
-    if (slow) b.queue[base + __popc(sm & lt_mask)] = slot;
-    __threadfence();
-    __syncwarp();
-    if (lane == 0) publish_in_order(b, kCtrQueuePublished, base, base + __popc(sm));
+    // the entry carries this launch's tag: a ticket holder that reads it knows it
+    // is not a leftover of an earlier launch
+    if (slow)
+      *reinterpret_cast<volatile unsigned long long *>(b.queue + base + __popc(sm & lt_mask)) =
+          ((unsigned long long)tag << 32) | (unsigned)slot;
   }
   __syncwarp();
 }

@@ -31,6 +31,7 @@ _SIGS = {
     "grand_engine_kernel_times": ([VP, VP, ctypes.POINTER(ctypes.c_float),
                                    ctypes.POINTER(ctypes.c_float)], ctypes.c_int),
     "grand_engine_batch_times": ([VP] + [ctypes.POINTER(ctypes.c_float)] * 4, ctypes.c_int),
+    "grand_engine_launch_stats": ([VP, VP, ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
     "grand_engine_sample": ([VP, ctypes.c_int, VP, ctypes.c_ulonglong, ctypes.c_ulonglong,
                              ctypes.c_int, VP, VP], ctypes.c_int),
     "grand_measure_int_peak": ([], ctypes.c_double),
@@ -152,6 +153,13 @@ class Engine:
         flip probabilities, d_records: num_shots * record_len int32)."""
         return self.lib.grand_engine_sample(self.h, code_id, d_p, seed, first_shot, num_shots,
                                             d_records, stream or None)
+
+    def launch_stats(self, stream=0):
+        """(settled by classification, per-shot path, Jobs, tiles, scratch words) of the
+        last device decode on `stream`."""
+        out = (ctypes.c_longlong * 5)()
+        rc = self.lib.grand_engine_launch_stats(self.h, stream or None, out)
+        return tuple(out) if rc == 0 else None
 
     def batch_times(self):
         """(h2d, triage, search, d2h) ms of the last host-buffer decode."""

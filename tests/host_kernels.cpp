@@ -418,24 +418,26 @@ static unsigned run_batch(DevBatch &b, int N) {
   const int max_jobs = std::max(N, 1);
   static std::vector<Job> jobs;
   jobs.assign(max_jobs, Job());
-  alignas(16) static unsigned long long small[32];
+  alignas(128) static unsigned long long small[kCtlAllocBytes / 8];
   memset(small, 0, sizeof(small));
   const unsigned long long scratch_words = 8ull << 20;
   static std::vector<uint32_t> scratch;
   scratch.assign(scratch_words, 0u);
-  static std::vector<int> deferred, queue;
+  static std::vector<int> deferred;
+  static std::vector<unsigned long long> queue;
   deferred.assign(N, 0);
-  queue.assign(std::max(N, 1), -1);
+  queue.assign(std::max(N, 1), 0ull);
   b.num_shots = N;
   b.ncr = ncr.data();
   b.jobs = jobs.data();
   b.max_jobs = max_jobs;
   b.counters = small;
-  b.status = reinterpret_cast<unsigned *>(reinterpret_cast<char *>(small) + 128);
+  b.status = reinterpret_cast<unsigned *>(reinterpret_cast<char *>(small) + kStatusByteOffset);
   b.scratch = scratch.data();
   b.scratch_words = scratch_words;
   b.deferred = deferred.data();
   b.queue = queue.data();
+  b.epoch = reinterpret_cast<unsigned *>(reinterpret_cast<char *>(small) + kCtlBytes);
   const char *fe = getenv("GRAND_EMU_FAST");
   b.fast = (fe && *fe == '0') ? 0 : 1;
   run_block(kDecodeWarps * 32, [&] {
@@ -447,8 +449,8 @@ static unsigned run_batch(DevBatch &b, int N) {
       fprintf(stderr, "shot %d deferred (status %u)\n", i, *b.status);
       exit(3);
     }
-  printf("ok %d shots, %llu jobs, %llu slow, status %u\n", N, small[kCtrJobsPublished] >> 40,
-         small[kCtrSlowDone], *b.status);
+  printf("ok %d shots, %llu jobs, %llu slow, status %u\n", N,
+         *ctr_ptr(small, kCtrJobs) >> 40, *ctr_ptr(small, kCtrSlowDone), *b.status);
   return *b.status;
 }
 
