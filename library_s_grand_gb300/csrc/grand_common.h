@@ -137,12 +137,11 @@ struct Seg {
   unsigned long long base;   // first global candidate index of this block within the shot
   unsigned long long count;  // C(tam, w)
   unsigned long long nprefix;// number of (w-1)-prefixes, C(tam-1, w-1)
-  unsigned long long ntiles; // tiles of 32 lanes x K prefixes
-  unsigned long long tile_lo;// first tile of this block within the job (search kernel)
-  unsigned long long njt;    // tiles the search kernel runs for this block (0: none)
-  const unsigned long long *cum; // run tiles: tiles before run c, c = 0..tam-1 (scratch)
-  int K;                     // prefixes per lane in a tile
-  int runs;                  // 1: register-blocked run tiles (w >= 3); 0: colex tiles (w <= 2)
+  unsigned long long ntiles; // light search: colex tiles of 32 lanes x K prefixes (w <= 2)
+  unsigned long long tile_lo;// first lookup tile of this block within the Job
+  unsigned long long njt;    // lookup tiles the Job's searchers run for this block (0: none)
+  int K;                     // light search: prefixes per lane in a tile
+  int runs;                  // light search: 1 run tiles (w >= 3), 0 colex tiles (w <= 2)
 };
 
 struct IterInfo {

@@ -7,22 +7,25 @@
 #include <cuda_runtime.h>
 
 #include "grand_device.cuh"
+#include "grand_lookup.cuh"
 
 namespace grand {
 
 constexpr int kDecodeWarps = 4;                 // warps per block of the decode kernel
 constexpr int kLightTam = 96;                   // largest active set the triage warp searches
 constexpr int kLightWords = kLightTam * 8;      // its staged column words (nwp <= 8)
-constexpr int kWarpStage = 1280;  // per search warp: staged column sketches, or the Job at its end
+// per search warp: the staged lookup block of an iteration, or the Job at its
+// end (the rest of the warp's area holds the syndrome and the degeneracy delta)
+constexpr int kWarpStage = 2720;
 constexpr int kTilesPerFetch = 4;  // most tiles a search warp draws at once
-constexpr int kRunKK = 8;       // prefixes per lane in a run tile (search kernel)
-constexpr int kRunKKLight = 4;  // the same inside the triage warp's light search
+constexpr int kRunKKLight = 4;  // prefixes per lane in a run tile of the triage warp's light search
 
 // Per-warp shared memory of the decode kernel.  A warp does one kind of work at
 // a time and reuses the same bytes for it: a shot's triage (the fields below), a
 // chunk's classification (FastArea, grand_triage.cuh) or search tiles (the first
-// kWarpStage words hold the staged sketches or a Job being finished, then the
-// syndrome and the degeneracy delta).
+// kWarpStage words hold the staged lookup block or a Job being finished, then
+// the syndrome and the degeneracy delta).  While a Job is published, the light
+// search's arrays (cols .. tmp) are the scratch that builds its lookup tables.
 struct alignas(128) WarpArea {
   uint32_t cols[kLightWords];
   uint32_t hcols[kLightTam];

@@ -2,8 +2,9 @@
 // of the persistent decode kernel (grand_decode.cuh).
 //
 // search_tiles: a warp evaluates a range of tiles (K colex prefixes per lane of
-//   one weight block of one Job) it drew from the launch's tile counter, stages
-//   the iteration's column sketches in its own shared-memory slice, publishes the
+//   one weight block of one Job, each probing the iteration's lookup tables,
+//   grand_lookup.cuh) it drew from the launch's tile counter, stages the
+//   iteration's lookup block in its own shared-memory slice, publishes the
 //   lowest matching global index (atomicMin) or the lowest {cost, rank} key
 //   (128-bit CAS), and the warp that completes a Job's last tile writes its
 //   result.  Tiles whose candidates all rank above an already-found match are
@@ -70,28 +71,27 @@ static __device__ Winner winner_ml(const Job &J) {
   return wn;
 }
 
-// Per-warp state carried from one drawn tile range to the next: the last Job,
-// weight block and run looked up (tiles of one draw are consecutive, so the
-// lookups are mostly reused) and which iteration's sketches are in the stage.
+// Per-warp state carried from one drawn tile range to the next: the last Job
+// and weight block looked up (tiles of one draw are consecutive, so the lookups
+// are mostly reused) and which iteration's lookup block is in the stage.
 struct SearchCache {
   int st_job, st_it;
-  int cj, cs, cc;
-  unsigned long long cj_lo, cj_hi, cs_lo, cs_hi, cc_lo, cc_hi;
+  int cj, cs;
+  unsigned long long cj_lo, cj_hi, cs_lo, cs_hi;
   Job *Jp;
   const DevCode *cdp;
   SegView sv;
-  int s_runs, s_iter, s_ml, s_prob;
-  const unsigned long long *s_cum;
+  LookView lk;
+  int s_iter, s_ml, s_prob;
   __device__ void reset() {
     st_job = st_it = -1;
-    cj = cs = cc = -1;
-    cj_lo = cj_hi = cs_lo = cs_hi = cc_lo = cc_hi = 0;
+    cj = cs = -1;
+    cj_lo = cj_hi = cs_lo = cs_hi = 0;
     Jp = nullptr;
     cdp = nullptr;
-    s_runs = s_iter = s_ml = s_prob = 0;
-    s_cum = nullptr;
+    s_iter = s_ml = s_prob = 0;
   }
-  // the stage was used for other work: its sketches are gone
+  // the stage was used for other work: its tables are gone
   __device__ void stage_lost() { st_job = st_it = -1; }
 };
 
@@ -143,24 +143,24 @@ __device__ void search_tiles(const DevBatch &b, unsigned long long t0, unsigned 
       c.cs = sg;
       c.cs_lo = S.tile_lo;
       c.cs_hi = c.cs_lo + S.njt;
-      c.cc = -1;
-      c.s_runs = S.runs;
-      c.s_cum = S.cum;
       c.s_iter = S.iter;
       c.s_ml = MLK && c.cdp->variant == kMl;
       c.s_prob = c.cdp->variant == kProb;
-      // the scans read only the column sketches: those are staged (the full
-      // columns are read from the Job's scratch for the rare exact tests)
-      const bool staged = I.tam <= kWarpStage;
-      c.sv = SegView{staged ? stage : I.hcols, I.cols, I.llr, J.hs, I.tam, S.w, S.K, c.cdp->nwp,
+      // the iteration's lookup block (sketches, filter, buckets) is staged when
+      // it fits; the full columns stay in the Job's scratch for the exact tests
+      const LookLayout L = look_layout(I.tam, kWarpStage);
+      const bool staged = L.words <= kWarpStage;
+      const uint32_t *blk = staged ? stage : I.hcols;
+      c.sv = SegView{blk, I.cols, I.llr, J.hs, I.tam, S.w, kLookK, c.cdp->nwp,
                      c.cdp->nw, S.nprefix, S.base};
+      c.lk = look_view(blk, L);
       if (c.st_job != c.cj || c.st_it != S.iter) {
         __syncwarp();
         if (staged) {
           const uint4 *src = reinterpret_cast<const uint4 *>(I.hcols);
           uint4 *dst = reinterpret_cast<uint4 *>(stage);
-          const int n4 = (I.tam + 3) / 4;
-          for (int i = lane; i < n4; i += 32) dst[i] = src[i];
+          const int n4 = L.words / 4;
+          for (int i = lane; i < n4; i += 32) dst[i] = __ldcg(src + i);
         }
         sw[lane] = J.sw[lane];
         __syncwarp();
@@ -179,22 +179,8 @@ __device__ void search_tiles(const DevBatch &b, unsigned long long t0, unsigned 
       LaneBest lb;
       lb.reset();
       const unsigned long long st = lt - c.cs_lo;
-      if (c.s_runs) {
-        if (c.cc < 0 || st < c.cc_lo || st >= c.cc_hi) {
-          // run c holding segment tile st: largest c with cum[c] <= st
-          const unsigned long long *cum = c.s_cum;
-          const int clo = warp_search_le(0, c.sv.tam - 2, st, [&](int i) { return cum[i]; });
-          c.cc = clo;
-          c.cc_lo = c.s_cum[clo];
-          c.cc_hi = c.cc_lo + run_tiles(b.ncr, clo, c.sv.w, kRunKK);
-        }
-        const unsigned long long r0 = (st - c.cc_lo) * (32ull * kRunKK);
-        if (c.s_ml) eval_run_tile<kRunKK, true>(c.sv, b.ncr, sw, c.cc, r0, lb);
-        else eval_run_tile<kRunKK, false>(c.sv, b.ncr, sw, c.cc, r0, lb);
-      } else {
-        if (c.s_ml) eval_tile<true>(c.sv, b.ncr, sw, st, lb);
-        else eval_tile<false>(c.sv, b.ncr, sw, st, lb);
-      }
+      if (c.s_ml) eval_lookup_tile<kLookK, true>(c.sv, c.lk, b.ncr, sw, st, lb);
+      else eval_lookup_tile<kLookK, false>(c.sv, c.lk, b.ncr, sw, st, lb);
       // a tile without a match (nearly every tile) skips the reductions
       if (!c.s_ml) {
         if (__any_sync(kFull, lb.g != kNone)) {

@@ -75,10 +75,10 @@ static __device__ int plan_next(const DevCode &cd, int tam0, int tam1, int tam2,
       S.base = P.gbase + tot;
       S.nprefix = binom(tam - 1, w - 1);
       S.runs = w >= 3 ? 1 : 0;
-      S.cum = nullptr;
-      S.K = S.runs ? kRunKK : tile_k;
-      // run-tile counts are built by the warp when a Job is published; colex
-      // blocks (w <= 2) have at most tam - 1 prefixes, so a 32-bit division suffices
+      S.K = S.runs ? kRunKKLight : tile_k;
+      // tile counts of the light search: run tiles are counted run by run as
+      // they are walked; colex blocks (w <= 2) have at most tam - 1 prefixes, so
+      // a 32-bit division suffices.  A Job's blocks are searched in lookup tiles.
       S.ntiles = S.runs ? 0ull
                         : (unsigned long long)(((unsigned)S.nprefix + 32u * (unsigned)S.K - 1u) /
                                                (32u * (unsigned)S.K));
@@ -708,15 +708,10 @@ __device__ void triage_shot(const DevBatch &b, int slot, WarpArea &A, PlanState 
     unsigned long long words = 0;
     for (int ii = heavy_from; ii < J.n_it; ++ii) {
       const unsigned long long tm = (unsigned long long)J.it[ii].tam;
-      words += (tm * cd.nwp + 3ull) & ~3ull;              // columns
-      words += (tm + 3ull) & ~3ull;                       // column sketches
+      words += (tm * cd.nwp + 3ull) & ~3ull;                            // columns
+      words += (unsigned long long)look_layout((int)tm, kWarpStage).words;  // lookup block
       words += ((ml ? 2ull : 1ull) * tm + 3ull) & ~3ull;  // positions (+ sort buffer)
       if (ml) words += (tm + 3ull) & ~3ull;               // LLRs
-    }
-    for (int s = 0; s < J.nseg; ++s) {
-      const Seg &S = J.seg[s];
-      if (S.runs && !S.dup && S.iter >= heavy_from)
-        words += (2ull * (unsigned long long)J.it[S.iter].tam + 3ull) & ~3ull;  // run-tile table
     }
     words += 128;  // supplied bits
     // whole 128-byte lines, so no line is shared with another Job's data
@@ -751,8 +746,9 @@ __device__ void triage_shot(const DevBatch &b, int slot, WarpArea &A, PlanState 
       const unsigned long long tm = (unsigned long long)I.tam;
       uint32_t *cols = sp;
       sp += (tm * cd.nwp + 3ull) & ~3ull;
-      uint32_t *hcols = sp;
-      sp += (tm + 3ull) & ~3ull;
+      const LookLayout LL = look_layout((int)tm, kWarpStage);
+      uint32_t *hcols = sp;  // the lookup block starts with the column sketches
+      sp += (unsigned long long)LL.words;
       int *pos = reinterpret_cast<int *>(sp);
       int *tmp = pos + tm;
       sp += ((ml ? 2ull : 1ull) * tm + 3ull) & ~3ull;
@@ -762,6 +758,8 @@ __device__ void triage_shot(const DevBatch &b, int slot, WarpArea &A, PlanState 
         sp += (tm + 3ull) & ~3ull;
       }
       stage_iteration<MLK>(cd, A.am[I.src], I.tam, pos, tmp, cols, hcols, llr);
+      // the light search's arrays are free now: the table builder's scratch
+      build_lookup(hcols, I.tam, LL, A.cols);
       if (lane == 0) {
         I.pos = pos;
         I.cols = cols;
@@ -778,37 +776,11 @@ __device__ void triage_shot(const DevBatch &b, int slot, WarpArea &A, PlanState 
       }
       __syncwarp();
     }
-    // run-tile tables: cum[c] = run tiles before run c (warp prefix scan)
-    for (int sgi = 0; sgi < J.nseg; ++sgi) {
-      Seg &S = J.seg[sgi];
-      if (!S.runs || S.dup || S.iter < heavy_from) continue;
-      const int tam = J.it[S.iter].tam;
-      unsigned long long *cum = reinterpret_cast<unsigned long long *>(sp);
-      sp += (2ull * (unsigned long long)tam + 3ull) & ~3ull;
-      unsigned long long carry = 0;
-      for (int c0 = 0; c0 < tam; c0 += 32) {
-        const int c = c0 + lane;
-        const unsigned long long nt = (c <= tam - 2) ? run_tiles(b.ncr, c, S.w, kRunKK) : 0ull;
-        unsigned long long incl = nt;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const unsigned long long u = __shfl_up_sync(kFull, incl, o);
-          if (lane >= o) incl += u;
-        }
-        if (c < tam) cum[c] = carry + incl - nt;
-        carry += __shfl_sync(kFull, incl, 31);
-      }
-      if (lane == 0) {
-        S.cum = cum;
-        S.ntiles = carry;
-      }
-      __syncwarp();
-    }
     if (lane == 0) {
       J.it_lo = heavy_from;
       for (int sgi = 0; sgi < J.nseg; ++sgi) {
         Seg &S = J.seg[sgi];
-        S.njt = (S.dup || S.iter < heavy_from) ? 0ull : S.ntiles;
+        S.njt = (S.dup || S.iter < heavy_from) ? 0ull : lookup_tiles(S.nprefix);
         S.tile_lo = ntl;
         ntl += S.njt;
       }
