@@ -109,7 +109,18 @@ int grand_engine_kernel_times(GrandEngine *engine, void *stream, float *reset_ms
  * grand_engine_sync_status): out[0] shots settled by classification (empty
  * syndromes, one-position weight-1 matches), out[1] shots that took the
  * per-shot path, out[2] Jobs published, out[3] search tiles of those Jobs,
- * out[4] scratch words staged for them. */
+ * out[4] scratch words staged for them.  With GRAND_PROFILE=1 in the
+ * environment when the engine was created, out[5..8] are the warp-nanoseconds
+ * the decode kernel's warps spent classifying, on the per-shot path, on search
+ * tiles and waiting for work, out[9..12] when the last of each ended (ns after
+ * the first warp started; -1: none), out[13] the number of work steps and
+ * out[14..23] a finer split of the warp-nanoseconds: classification (records
+ * read and syndromes formed, one-position test, results and queue), per-shot
+ * path (record packed, flagged-check counts, planning and light search, Job
+ * staging and publication, result written) and search (Job and block lookup
+ * with staging, completed Jobs' results) and out[24..27] the Job publications
+ * split into reservations, staging, the Job written and the steps that make it
+ * searchable; otherwise those entries are 0 / -1.  `out` holds 28 entries. */
 int grand_engine_launch_stats(GrandEngine *engine, void *stream, long long *out);
 
 /* Times of the last host-buffer decode (grand_engine_decode / _decode_plain):

@@ -92,7 +92,29 @@ enum Counter {
   kCtrSlowDone = 7,       // per-shot-path shots finished (their Jobs published)
   kCtrWarpsDone = 8,      // warps that left the kernel (the last advances the epoch)
   kCtrSettled = 10,       // shots settled by classification (statistics)
+  kCtrProfSums = 11,      // profile (DevBatch::profile): warp-ns per kind of work, steps
+  kCtrProfEnds = 13,      // profile: latest end per kind of work, ~(first warp start)
+  kCtrProfMore = 14,      // profile: the Job publication's steps (kProfPub*)
 };
+// Words of the two profile lines: kinds of work in the order of the decode
+// kernel's steps (classification chunks, per-shot path, search tiles, waiting),
+// then the number of steps (sums line) and the complemented start (ends line).
+// Sums words 6.. split the work further: classification (records read and
+// syndromes formed; one-position test; results and queue), per-shot path (record
+// packed; flagged-check counts; planning and light search; Job staging and
+// publication; result written) and search (Job / block lookup and staging; a
+// completed Job's result).
+enum ProfWord { kProfChunk = 0, kProfShot = 1, kProfTiles = 2, kProfWait = 3, kProfKinds = 4,
+                kProfSteps = 4, kProfStart = 5,
+                kProfChunkRead = 6, kProfChunkTest = 7, kProfChunkWrite = 8,
+                kProfShotPack = 9, kProfShotCounts = 10, kProfShotLight = 11,
+                kProfShotPublish = 12, kProfShotFinish = 13,
+                kProfTileSetup = 14, kProfTileFinish = 15, kProfDetails = 10 };
+// Words of the kCtrProfMore line: a Job's publication split into its scratch
+// and slot reservations, the staging of its iterations, the Job written, and
+// the fences and front advance that make it searchable.
+enum ProfPubWord { kProfPubReserve = 0, kProfPubStage = 1, kProfPubWrite = 2, kProfPubReady = 3,
+                   kProfPubWords = 4 };
 
 // Address of control word k.
 GRAND_HD inline unsigned long long *ctr_ptr(unsigned long long *counters, int k) {
@@ -216,6 +238,7 @@ struct DevBatch {
   unsigned long long *queue;     // num_shots entries: ((epoch + 1) << 32) | launch slot of a
                                  // shot that needs the per-shot path
   unsigned *epoch;               // the workspace's launch epoch (kCtlAllocBytes layout)
+  int profile;                   // 1: record per-phase times in the profile lines
   int fast;                      // 1: settle shots 32 at a time first (empty syndromes, and
                                  //    weight-1 matches of a one-position first iteration)
   int light_max_log2;            // light-path budget (candidates, log2)

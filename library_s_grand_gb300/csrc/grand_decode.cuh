@@ -38,12 +38,14 @@ constexpr int kDecodeMinBlocks = 4;  // resident blocks per SM the register budg
 
 // What a warp does next (decided by lane 0 from the control words, then
 // broadcast, so that the whole warp takes the same path).
-enum Step { kStepWait = 0, kStepChunk = 1, kStepShot = 2, kStepTiles = 3, kStepExit = 4 };
+enum Step { kStepWait = 0, kStepChunk = 1, kStepShot = 2, kStepTiles = 3, kStepExit = 4,
+            kStepHelp = 5 };
 
 template <bool MLK>
 __global__ void __launch_bounds__(kDecodeWarps * 32, kDecodeMinBlocks) decode_kernel(DevBatch b) {
   __shared__ WarpArea areas[kDecodeWarps];
   __shared__ PlanState plans[kDecodeWarps];
+  __shared__ TileView views[kDecodeWarps];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
   WarpArea &A = areas[wib];
@@ -59,6 +61,12 @@ __global__ void __launch_bounds__(kDecodeWarps * 32, kDecodeMinBlocks) decode_ke
   unsigned long long ticket = kNone;            // lane 0: a slow-queue ticket not yet used
   unsigned long long held_lo = 0, held_hi = 0;  // lane 0: tiles drawn and not yet run
   int polls = 0;
+  // profile (b.profile): lane 0 adds the time of each step to its kind's total
+  unsigned long long *psum = ctr_ptr(b.counters, kCtrProfSums);
+  unsigned long long *pend = ctr_ptr(b.counters, kCtrProfEnds);
+  const unsigned long long t_enter = b.profile ? global_ns() : 0ull;
+  unsigned long long t_busy = 0;
+  if (b.profile && lane == 0) atomicMax(pend + kProfStart, ~t_enter);
   for (;;) {
     int step = kStepWait;
     unsigned long long a0 = 0, a1 = 0, a2 = 0;
@@ -111,7 +119,7 @@ __global__ void __launch_bounds__(kDecodeWarps * 32, kDecodeMinBlocks) decode_ke
           const unsigned long long next = ld_ctr(b, kCtrNextTile);
           if (next < ptiles) {
             unsigned long long f = kTilesPerFetch;
-            while (f > 1ull && ptiles - next < 8ull * f * nwarps) f >>= 1;
+            while (f > 1ull && ptiles - next < 2ull * f * nwarps) f >>= 1;
             held_lo = atomicAdd(ctr_ptr(b.counters, kCtrNextTile), f);
             held_hi = held_lo + f;
           }
@@ -142,13 +150,17 @@ __global__ void __launch_bounds__(kDecodeWarps * 32, kDecodeMinBlocks) decode_ke
             if (held_lo >= total) held_lo = held_hi = 0;
             if (held_lo >= held_hi && ld_ctr(b, kCtrNextTile) >= total) step = kStepExit;
           } else {
-            advance_front(b, tag);  // a publisher's advance can lose a race: help it
+            step = kStepHelp;  // a publisher's advance can lose a race: help it
           }
         }
       }
     }
     step = __shfl_sync(kFull, step, 0);
     if (step == kStepExit) break;
+    if (step == kStepHelp) {
+      advance_front(b, tag);
+      step = kStepWait;
+    }
     if (step == kStepWait) {
       if (++polls > kWaitPolls) {
         if (lane == 0) atomicOr(b.status, kStatusWaitLimit);
@@ -158,6 +170,7 @@ __global__ void __launch_bounds__(kDecodeWarps * 32, kDecodeMinBlocks) decode_ke
       continue;
     }
     polls = 0;
+    const unsigned long long t_step = b.profile ? global_ns() : 0ull;
     a0 = __shfl_sync(kFull, a0, 0);
     if (step == kStepChunk) {
       classify_chunk<MLK>(b, (int)a0, A, tag);
@@ -176,8 +189,21 @@ __global__ void __launch_bounds__(kDecodeWarps * 32, kDecodeMinBlocks) decode_ke
     } else {
       a1 = __shfl_sync(kFull, a1, 0);
       a2 = __shfl_sync(kFull, a2, 0);
-      search_tiles<MLK>(b, a0, a1, a2, A, cache);
+      search_tiles<MLK>(b, a0, a1, a2, A, cache, views[wib]);
     }
+    if (b.profile && lane == 0) {
+      const unsigned long long t = global_ns();
+      const int kind = step == kStepChunk ? kProfChunk : (step == kStepShot ? kProfShot : kProfTiles);
+      atomicAdd(psum + kind, t - t_step);
+      atomicAdd(psum + kProfSteps, 1ull);
+      atomicMax(pend + kind, t);
+      t_busy += t - t_step;
+    }
+  }
+  if (b.profile && lane == 0) {
+    const unsigned long long t = global_ns();
+    atomicAdd(psum + kProfWait, t - t_enter - t_busy);
+    atomicMax(pend + kProfWait, t);
   }
   // the last warp to leave advances the epoch for the next launch
   __syncwarp();

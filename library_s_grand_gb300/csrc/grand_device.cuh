@@ -340,8 +340,19 @@ __device__ __forceinline__ void unrank2(unsigned long long r, int &y0, int &y1) 
   y0 = (int)(r - (unsigned long long)v * (v - 1) / 2);
 }
 
+// Largest v in [lo, hi] with C(v, k) <= q, from the estimate C(v, k) ~
+// (v - (k - 1) / 2)^k / k! corrected with computed binomials (no table loads).
+__device__ __forceinline__ int binom_floor(unsigned long long q, int k, int lo, int hi) {
+  const float fact = k == 4 ? 24.0f : (k == 5 ? 120.0f : (k == 3 ? 6.0f : (k == 2 ? 2.0f : 1.0f)));
+  int v = (int)(powf(fact * (float)q, 1.0f / (float)k) + 0.5f * (float)(k - 1));
+  v = v < lo ? lo : (v > hi ? hi : v);
+  while (v > lo && binom(v, k) > q) --v;
+  while (v < hi && binom(v + 1, k) <= q) ++v;
+  return v;
+}
+
 // Colex unranking of a kk-subset of [0, c): closed forms for kk <= 3 (weights 3
-// to 5, the common case), the binomial-table search otherwise.
+// to 5, the common case), estimated and corrected binomial searches otherwise.
 __device__ __forceinline__ void sub_unrank(const unsigned long long *t, unsigned long long r,
                                            int kk, int c, int (&y)[5]) {
   if (kk == 1) {
@@ -358,7 +369,16 @@ __device__ __forceinline__ void sub_unrank(const unsigned long long *t, unsigned
     y[2] = v;
     unrank2(r - c3(v), y[0], y[1]);
   } else {
-    colex_unrank(t, r, kk, c - 1, y);
+    int hi = c - 1;
+#pragma unroll
+    for (int i = 4; i >= 0; --i) {
+      if (i < kk) {
+        const int v = binom_floor(r, i + 1, i, hi);
+        r -= binom(v, i + 1);
+        y[i] = v;
+        hi = v - 1;
+      }
+    }
   }
 }
 

@@ -267,6 +267,7 @@ int grand_engine_decode_device(GrandEngine *e, int num_shots, const int *d_shot_
   b.queue = shot_queue(slot->d_deferred, num_shots);
   b.epoch = (unsigned *)((char *)slot->d_small + kCtlBytes);
   b.fast = e->tn.fast;
+  b.profile = e->tn.profile;
   b.light_max_log2 = e->tn.light_max_log2;
   b.tile_k = e->tn.tile_k;
   for (const DevCode &c : e->codes) b.has_ml |= c.variant == kMl;
@@ -349,6 +350,18 @@ int grand_engine_launch_stats(GrandEngine *e, void *stream, long long *out) {
   out[2] = (long long)(c[kCtrJobs * kCtrStride] >> 40);
   out[3] = (long long)(c[kCtrJobs * kCtrStride] & ((1ull << 40) - 1ull));
   out[4] = (long long)c[kCtrScratchTop * kCtrStride];
+  // phase profile (GRAND_PROFILE=1): times in ns from the first warp's start
+  const unsigned long long *pa = c.data() + kCtrProfSums * kCtrStride;
+  const unsigned long long *pb = c.data() + kCtrProfEnds * kCtrStride;
+  const unsigned long long t0 = ~pb[kProfStart];
+  for (int i = 0; i < kProfKinds; ++i) {
+    out[5 + i] = (long long)pa[i];                                        // warp-ns spent
+    out[5 + kProfKinds + i] = pb[i] ? (long long)(pb[i] - t0) : -1;       // last end
+  }
+  out[5 + 2 * kProfKinds] = (long long)pa[kProfSteps];
+  for (int i = 0; i < kProfDetails; ++i) out[14 + i] = (long long)pa[kProfChunkRead + i];
+  const unsigned long long *pm = c.data() + kCtrProfMore * kCtrStride;
+  for (int i = 0; i < kProfPubWords; ++i) out[24 + i] = (long long)pm[i];
   return 0;
 }
 

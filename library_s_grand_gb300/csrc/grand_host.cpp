@@ -40,6 +40,7 @@ Tuning &tuning() {
     if (const char *s = getenv("GRAND_SEARCH_GRID_MULT")) x.search_grid_mult = std::max(0, atoi(s));
     if (const char *s = getenv("GRAND_ZERO_COPY")) x.zero_copy = atoi(s) != 0;
     if (const char *s = getenv("GRAND_FAST")) x.fast = atoi(s) != 0;
+    if (const char *s = getenv("GRAND_PROFILE")) x.profile = atoi(s) != 0;
     return x;
   }();
   return t;
@@ -497,6 +498,7 @@ int run_batch(Context *ctx, Workspace *ws, const BatchRequest &req, BatchTiming 
   b.queue = shot_queue(ws->d_deferred, N);
   b.epoch = (unsigned *)((char *)ws->d_small + kCtlBytes);
   b.fast = tn.fast;
+  b.profile = tn.profile;
   b.light_max_log2 = tn.light_max_log2;
   b.tile_k = tn.tile_k;
   for (const DevCode &c : req.codes) b.has_ml |= c.variant == kMl;

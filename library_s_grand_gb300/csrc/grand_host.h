@@ -149,6 +149,7 @@ struct Tuning {
   int fast = 1;              // settle shots 32 at a time before the per-shot path (GRAND_FAST)
   int zero_copy = 1;         // read records / write results in the caller's host memory
                              // when the device can access pageable memory (GRAND_ZERO_COPY)
+  int profile = 0;           // the decode kernel records per-phase times (GRAND_PROFILE)
 };
 Tuning &tuning();  // process defaults (GRAND_LIGHT_LOG2, GRAND_TILE_K, GRAND_SEARCH_GRID_MULT)
 

@@ -5,6 +5,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <stddef.h>
 
 #include "grand_device.cuh"
 #include "grand_lookup.cuh"
@@ -17,7 +18,7 @@ constexpr int kLightWords = kLightTam * 8;      // its staged column words (nwp 
 // per search warp: the staged lookup block of an iteration, or the Job at its
 // end (the rest of the warp's area holds the syndrome and the degeneracy delta)
 constexpr int kWarpStage = 2720;
-constexpr int kTilesPerFetch = 4;  // most tiles a search warp draws at once
+constexpr int kTilesPerFetch = 16;  // most tiles a search warp draws at once
 constexpr int kRunKKLight = 4;  // prefixes per lane in a run tile of the triage warp's light search
 
 // Per-warp shared memory of the decode kernel.  A warp does one kind of work at
@@ -38,6 +39,12 @@ struct alignas(128) WarpArea {
   uint32_t delta[kMaxCols / 32];
   Job job;
 };
+
+// Words of the light search's arrays (cols .. tmp), the publishing warp's
+// working space for a heavy iteration's positions.
+constexpr int kPublishWords = kLightWords + 4 * kLightTam;
+static_assert(offsetof(WarpArea, sw) - offsetof(WarpArea, cols) == sizeof(uint32_t) * kPublishWords,
+              "the light search's arrays are contiguous");
 
 // Planner state of one shot (resumable walk over upstream's iteration loop).
 struct PlanState {
@@ -65,21 +72,52 @@ __device__ __forceinline__ unsigned long long ld_ctr(const DevBatch &b, int ctr)
   return *reinterpret_cast<volatile unsigned long long *>(ctr_ptr(b.counters, ctr));
 }
 
-// Lane 0.  Jobs are searchable from the front: the leading Jobs whose ready words
-// carry this launch's tag.  Whoever finds the Job at the front written moves the
-// front past it (and on, while the next is written too).  A publisher calls this
-// after marking its Job ready, so every written Job is passed: the publisher of
-// the last Job to become ready finds all before it written.
+// Profile (DevBatch::profile): lane 0 adds the time since t0 to profile sums
+// word w; returns the current time (0 when not profiling).
+__device__ __forceinline__ unsigned long long prof_lap(const DevBatch &b, int w,
+                                                       unsigned long long t0,
+                                                       int line = kCtrProfSums) {
+  if (!b.profile) return 0ull;
+  const unsigned long long t = global_ns();
+  if ((threadIdx.x & 31) == 0) atomicAdd(ctr_ptr(b.counters, line) + w, t - t0);
+  return t;
+}
+
+// The whole warp.  Jobs are searchable from the front: the leading Jobs whose
+// ready words carry this launch's tag.  Whoever finds Jobs at the front written
+// moves the front past them: the warp reads the ready words of the next 32 Jobs
+// at once and passes the written run among them (their tiles summed across the
+// lanes) with one compare-and-swap, so a long run of Jobs published together
+// costs a few round trips, not one per Job.  A publisher calls this after
+// marking its Job ready, so every written Job is passed: the publisher of the
+// last Job to become ready finds all before it written.
 __device__ __forceinline__ void advance_front(const DevBatch &b, unsigned tag) {
-  unsigned long long f = ld_ctr(b, kCtrFront);
-  for (int guard = 0; guard < (1 << 20); ++guard) {
-    const unsigned long long j = f >> 40;
-    if (j >= (ld_ctr(b, kCtrJobs) >> 40) || j >= (unsigned long long)b.max_jobs) return;
-    const Job *J = b.jobs + j;
-    if (*reinterpret_cast<const volatile unsigned *>(&J->ready) != tag) return;
-    const unsigned long long nt = *reinterpret_cast<const volatile unsigned long long *>(&J->ntiles);
-    const unsigned long long seen = atomicCAS(ctr_ptr(b.counters, kCtrFront), f, f + (1ull << 40) + nt);
-    f = seen == f ? f + (1ull << 40) + nt : seen;
+  const int lane = threadIdx.x & 31;
+  unsigned long long f = 0, lim = 0;
+  if (lane == 0) {
+    f = ld_ctr(b, kCtrFront);
+    lim = ld_ctr(b, kCtrJobs) >> 40;
+    if (lim > (unsigned long long)b.max_jobs) lim = (unsigned long long)b.max_jobs;
+  }
+  f = __shfl_sync(kFull, f, 0);
+  lim = __shfl_sync(kFull, lim, 0);
+  for (int guard = 0; guard < (1 << 16); ++guard) {
+    const unsigned long long j = (f >> 40) + (unsigned long long)lane;
+    const bool ready =
+        j < lim && *reinterpret_cast<const volatile unsigned *>(&b.jobs[j].ready) == tag;
+    const unsigned m = __ballot_sync(kFull, ready);
+    const int run = (m == kFull) ? 32 : __ffs(~m) - 1;  // written Jobs at the front
+    if (run == 0) return;
+    unsigned long long nt =
+        lane < run ? *reinterpret_cast<const volatile unsigned long long *>(&b.jobs[j].ntiles) : 0ull;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) nt += __shfl_xor_sync(kFull, nt, o);
+    unsigned long long seen = 0;
+    if (lane == 0)
+      seen = atomicCAS(ctr_ptr(b.counters, kCtrFront), f,
+                       f + ((unsigned long long)run << 40) + nt);
+    seen = __shfl_sync(kFull, seen, 0);
+    f = seen == f ? f + ((unsigned long long)run << 40) + nt : seen;
   }
 }
 

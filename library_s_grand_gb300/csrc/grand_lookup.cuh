@@ -12,25 +12,29 @@
 // answer -- the lowest-rank match, or for ML every match's cost -- is the scan's.
 // A prefix costs O(1) whatever the number of its candidates (tam - 1 - max(P)).
 //
-// Per heavy iteration the Job's scratch holds one contiguous lookup block, built
-// once by the publishing warp and copied into a search warp's shared-memory
-// stage when the warp starts on that iteration:
+// A search warp that starts on an iteration copies the column sketches from the
+// Job's scratch into its shared-memory stage and builds the tables there, so the
+// lookup block of an iteration is (an active set too large for the stage has
+// its block built once, in the scratch, by the publishing warp):
 //   hc     tam column sketches (in active-list order)
-//   filt   a 2^F-bit filter: bit (hc & (2^F - 1)) set for every column
-//   bst    2^B + 1 bucket starts (u16): the entries of bucket b (top B bits of the
-//          sketch) are key/pos[bst[b] .. bst[b+1])
+//   filt   a 2^F-bit blocked Bloom filter: each column sets three bits of one
+//          32-bit word (word = low F-5 bits of its sketch, bit positions = the
+//          next three 5-bit fields)
+//   bst    2^B + 1 bucket bounds (u32): the entries of bucket b (top B bits of
+//          the sketch) are key/pos[bst[b] .. bst[b+1])
 //   key    the tam sketches grouped by bucket
 //   pos    their active-list indices (u16)
-// A probe reads one filter word; only when its bit is set (about tam / 2^F of
-// prefixes that match nothing) does it walk the bucket.  Filter and buckets use
-// disjoint bits of the sketch (F + B <= 26).
+// A probe reads one filter word; only when all three of its bits are set (for a
+// prefix that matches nothing, about (3 tam / 2^F)^3: once per tens of thousands
+// of prefixes at tam ~ 100) does it walk the bucket, so the lanes of a warp
+// rarely wait for one another there.
 #pragma once
 
 #include "grand_device.cuh"
 
 namespace grand {
 
-constexpr int kLookK = 16;        // prefixes per lane in a lookup tile
+constexpr int kLookK = 32;        // prefixes per lane in a lookup tile
 constexpr int kLookMaxF = 15;     // largest filter (2^15 bits = 4 KB)
 constexpr int kLookMinF = 10;
 
@@ -56,9 +60,9 @@ GRAND_HD inline LookLayout look_layout(int tam, int cap_words) {
   L.B = ceil_log2i(tam);
   if (L.B < 1) L.B = 1;
   const int nb = 1 << L.B;
-  const int bst_words = ((nb + 2) / 2 + 3) & ~3;
+  const int bst_words = (nb + 2 + 3) & ~3;
   const int pos_words = ((tam + 1) / 2 + 3) & ~3;
-  int F = ceil_log2i(tam) + 7;
+  int F = ceil_log2i(tam) + 8;
   if (F > kLookMaxF) F = kLookMaxF;
   if (F < kLookMinF) F = kLookMinF;
   for (;;) {
@@ -77,71 +81,58 @@ GRAND_HD inline LookLayout look_layout(int tam, int cap_words) {
   }
 }
 
+// The three filter bits of sketch h (in the word h & (2^(F-5) - 1)).
+GRAND_HD inline uint32_t bloom_bits(uint32_t h, int F) {
+  return (1u << ((h >> (F - 5)) & 31u)) | (1u << ((h >> F) & 31u)) | (1u << ((h >> (F + 5)) & 31u));
+}
+
 // Build the tables of a block whose first tam words already hold the column
-// sketches (one warp; T is shared scratch of at least max(2^(F-5), 2^(B-1) + 1)
-// words).  Entries of one bucket land in any order: a probe checks them all.
-__device__ __forceinline__ void build_lookup(uint32_t *blk, int tam, const LookLayout &L,
-                                             uint32_t *T) {
+// sketches (one warp; the block in shared memory, or in the scratch for an
+// active set too large for the stage).  The bucket bounds double as counters:
+// bst[b + 1] counts bucket b, becomes its start after the scan and its end (the
+// next bucket's start) after the scatter, with bst[0] = 0 throughout.  Entries
+// of one bucket land in any order: a probe checks them all.
+__device__ __forceinline__ void build_lookup(uint32_t *blk, int tam, const LookLayout &L) {
   const int lane = threadIdx.x & 31;
   uint32_t *filt = blk + L.o_filt;
-  uint16_t *bst = reinterpret_cast<uint16_t *>(blk + L.o_bst);
+  uint32_t *bst = blk + L.o_bst;
   uint32_t *key = blk + L.o_key;
   uint16_t *pos = reinterpret_cast<uint16_t *>(blk + L.o_pos);
   const int fw = 1 << (L.F - 5);
-  const uint32_t fmask = (1u << L.F) - 1u;
   const int shift = 32 - L.B;
   const int nb = 1 << L.B;
-
-  // filter
-  for (int i = lane; i < fw; i += 32) T[i] = 0u;
+  for (int i = lane; i < fw; i += 32) filt[i] = 0u;
+  for (int i = lane; i < nb + 2; i += 32) bst[i] = 0u;
   __syncwarp();
-  for (int i = lane; i < tam; i += 32) {
-    const uint32_t f = blk[i] & fmask;
-    atomicOr(&T[f >> 5], 1u << (f & 31u));
-  }
-  __syncwarp();
-  for (int i = lane; i < fw; i += 32) filt[i] = T[i];
-  __syncwarp();
-
-  // bucket sizes, 16 bits each (two buckets per word; sizes and starts stay
-  // below 2^16 because tam <= 2048)
-  const int nbw = (nb + 1) >> 1;
-  for (int i = lane; i <= nbw; i += 32) T[i] = 0u;
-  __syncwarp();
-  for (int i = lane; i < tam; i += 32) {
-    const uint32_t bk = blk[i] >> shift;
-    atomicAdd(&T[bk >> 1], 1u << ((bk & 1u) * 16u));
-  }
-  __syncwarp();
-  // exclusive scan in bucket order: each lane an even-sized run of buckets (so
-  // no two lanes touch one word), then the lanes' totals across the warp
-  const int per = nb / 32 > 2 ? nb / 32 : 2;
-  const int b0 = lane * per;
-  int mine = 0;
-  for (int bk = b0; bk < b0 + per && bk < nb; ++bk) mine += (T[bk >> 1] >> ((bk & 1) * 16)) & 0xffffu;
-  int incl = mine;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const int u = __shfl_up_sync(kFull, incl, o);
-    if (lane >= o) incl += u;
-  }
-  int run = incl - mine;
-  for (int bk = b0; bk < b0 + per && bk < nb; ++bk) {
-    const unsigned sh = (unsigned)(bk & 1) * 16u;
-    const int cnt = (int)((T[bk >> 1] >> sh) & 0xffffu);
-    bst[bk] = (uint16_t)run;
-    T[bk >> 1] = (T[bk >> 1] & ~(0xffffu << sh)) | ((uint32_t)run << sh);  // the bucket's cursor
-    run += cnt;
-  }
-  if (lane == 0) bst[nb] = (uint16_t)tam;
-  __syncwarp();
-  // scatter
   for (int i = lane; i < tam; i += 32) {
     const uint32_t h = blk[i];
-    const uint32_t bk = h >> shift;
-    const unsigned sh = (bk & 1u) * 16u;
-    const uint32_t old = atomicAdd(&T[bk >> 1], 1u << sh);
-    const int slot = (int)((old >> sh) & 0xffffu);
+    atomicOr(&filt[h & (uint32_t)(fw - 1)], bloom_bits(h, L.F));
+    atomicAdd(&bst[(h >> shift) + 1u], 1u);
+  }
+  __syncwarp();
+  // exclusive scan of the counts in place: each lane a run of buckets, then the
+  // lanes' totals across the warp
+  const int per = nb >= 32 ? nb / 32 : 1;
+  const int b0 = 1 + lane * per;
+  const int b1 = (b0 + per < nb + 1) ? b0 + per : nb + 1;
+  uint32_t mine = 0u;
+  for (int i = b0; i < b1; ++i) mine += bst[i];
+  uint32_t incl = mine;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t u = __shfl_up_sync(kFull, incl, o);
+    if (lane >= o) incl += u;
+  }
+  uint32_t run = incl - mine;
+  for (int i = b0; i < b1; ++i) {
+    const uint32_t c = bst[i];
+    bst[i] = run;
+    run += c;
+  }
+  __syncwarp();
+  for (int i = lane; i < tam; i += 32) {
+    const uint32_t h = blk[i];
+    const uint32_t slot = atomicAdd(&bst[(h >> shift) + 1u], 1u);
     key[slot] = h;
     pos[slot] = (uint16_t)i;
   }
@@ -151,36 +142,62 @@ __device__ __forceinline__ void build_lookup(uint32_t *blk, int tam, const LookL
 // Where a warp reads an iteration's lookup tables (its stage or the scratch).
 struct LookView {
   const uint32_t *filt;
-  const uint16_t *bst;
+  const uint32_t *bst;
   const uint32_t *key;
   const uint16_t *pos;
-  uint32_t fmask;
+  uint32_t wmask;  // filter word index mask, 2^(F-5) - 1
+  int F;
   int shift;
 };
 
 __device__ __forceinline__ LookView look_view(const uint32_t *blk, const LookLayout &L) {
   LookView v;
   v.filt = blk + L.o_filt;
-  v.bst = reinterpret_cast<const uint16_t *>(blk + L.o_bst);
+  v.bst = blk + L.o_bst;
   v.key = blk + L.o_key;
   v.pos = reinterpret_cast<const uint16_t *>(blk + L.o_pos);
-  v.fmask = (1u << L.F) - 1u;
+  v.wmask = (1u << (L.F - 5)) - 1u;
+  v.F = L.F;
   v.shift = 32 - L.B;
   return v;
 }
 
-// The candidates of prefix x[0..k-1] (largest element cl, sketch h = h(s) ^ h(P)):
-// every j > cl whose column sketch equals h, confirmed word by word.
+// Word i of a staged table at shared-memory address a (SH), or of p.
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+#ifdef GRAND_HOST_EMULATION
+  (void)p;
+  return 0u;
+#else
+  return (uint32_t)__cvta_generic_to_shared(p);
+#endif
+}
+// (Not volatile: the tables do not change while a tile is evaluated, so the
+// compiler may schedule and combine these loads freely inside the tile
+// function, which is never inlined into code that rewrites the stage.)
+template <bool SH>
+__device__ __forceinline__ uint32_t tab_word(const uint32_t *p, uint32_t a, uint32_t i) {
+#ifndef GRAND_HOST_EMULATION
+  if constexpr (SH) {
+    uint32_t v;
+    asm("ld.shared.u32 %0, [%1];" : "=r"(v) : "r"(a + 4u * i));
+    return v;
+  }
+#endif
+  (void)a;
+  return p[i];
+}
+
+// The candidates of prefix x[0..k-1] (largest element cl, sketch h = h(s) ^ h(P))
+// that passed the filter: every j > cl whose column sketch equals h, confirmed
+// word by word.
 template <bool ML>
-__device__ __forceinline__ void probe_prefix(const SegView &sv, const LookView &lk,
+__device__ __forceinline__ void probe_bucket(const SegView &sv, const LookView &lk,
                                              const unsigned long long *t, const uint32_t *sw,
                                              uint32_t h, const int (&x)[5], int k, int cl,
                                              LaneBest &lb) {
-  const uint32_t f = h & lk.fmask;
-  if (!((lk.filt[f >> 5] >> (f & 31u)) & 1u)) return;
   const uint32_t bk = h >> lk.shift;
-  const int e1 = lk.bst[bk + 1];
-  for (int e = lk.bst[bk]; e < e1; ++e) {
+  const int e1 = (int)lk.bst[bk + 1];
+  for (int e = (int)lk.bst[bk]; e < e1; ++e) {
     if (lk.key[e] != h) continue;
     const int j = lk.pos[e];
     if (j > cl && exact_match(sv, sw, x, k, j)) record_match<ML>(sv, t, x, k, j, lb);
@@ -190,76 +207,76 @@ __device__ __forceinline__ void probe_prefix(const SegView &sv, const LookView &
 // One lookup tile: lane l takes the K colex-consecutive prefixes
 // tile * 32K + l * K + [0, K) of the block's C(tam - 1, w - 1) prefixes (ascending
 // (w-1)-subsets of [0, tam - 1), so each has at least one j above it).  The
-// prefix sketch is updated incrementally: a colex step changes the lowest
-// element (one staged sketch load) and, rarely, the ones above it.
-template <int K, bool ML>
-__device__ __forceinline__ void eval_lookup_tile(const SegView &sv, const LookView &lk,
-                                                 const unsigned long long *t, const uint32_t *sw,
-                                                 unsigned long long tile, LaneBest &lb) {
+// prefix sketch is the upper elements' sketch hu = h(s) ^ hc[x1] ^ ... (kept in
+// a register) XOR hc[x0]: a colex step raises x0, and only when x0 meets x1 do
+// the upper elements advance (hu recomputed).  Per prefix: one staged sketch
+// load, one filter load and a three-bit test; a filter hit walks its bucket.
+// SH: the tables are in the warp's stage (explicit shared-memory loads).  Not
+// inlined: the scan gets the whole register budget instead of sharing it with
+// the scheduling state of the persistent kernel around it (sv and lk are the
+// warp's copies in shared memory).
+template <int K, bool ML, bool SH>
+__device__ __noinline__ LaneBest eval_lookup_tile(const SegView &sv, const LookView &lk,
+                                                  const unsigned long long *t, const uint32_t *sw,
+                                                  unsigned long long tile) {
+  LaneBest lb;
+  lb.reset();
   const int lane = threadIdx.x & 31;
   const int k = sv.w - 1;
   const int tam = sv.tam;
   const uint32_t *hc = sv.hcols;
+  const uint32_t hca = SH ? smem_addr(hc) : 0u, fa = SH ? smem_addr(lk.filt) : 0u;
+  const uint32_t wmask = lk.wmask;
+  const int F = lk.F;
   const uint32_t hs = sv.hs;
   const unsigned long long q = tile * (32ull * K) + (unsigned long long)lane * K;
-  if (q >= sv.nprefix) return;
+  if (q >= sv.nprefix) return lb;
   const int v = (sv.nprefix - q) < (unsigned long long)K ? (int)(sv.nprefix - q) : K;
   int x[5] = {0, 1, 2, 3, 4};
   if (k == 0) {  // weight 1: the empty prefix, every j
-    probe_prefix<ML>(sv, lk, t, sw, hs, x, 0, -1, lb);
-    return;
+    const uint32_t m = bloom_bits(hs, F);
+    if ((tab_word<SH>(lk.filt, fa, hs & wmask) & m) == m)
+      probe_bucket<ML>(sv, lk, t, sw, hs, x, 0, -1, lb);
+    return lb;
   }
   sub_unrank(t, q, k, tam - 1, x);
-  if (k == 1) {
-    for (int s = 0; s < v; ++s) {
-      probe_prefix<ML>(sv, lk, t, sw, hs ^ hc[x[0]], x, 1, x[0], lb);
-      ++x[0];
+  int x0 = x[0];
+  int xb = k >= 2 ? x[1] : tam - 1;  // x0 stays below this until the upper part moves
+  int top = x[0];                    // the largest element (k >= 2)
+  uint32_t hu = hs;
+#pragma unroll
+  for (int e = 1; e < 5; ++e)
+    if (e < k) {
+      hu ^= hc[x[e]];
+      top = x[e];
     }
-  } else if (k == 2) {
-    uint32_t h1 = hs ^ hc[x[1]];
-    for (int s = 0; s < v; ++s) {
-      probe_prefix<ML>(sv, lk, t, sw, h1 ^ hc[x[0]], x, 2, x[1], lb);
-      if (++x[0] == x[1]) {
-        x[0] = 0;
-        h1 = hs ^ hc[++x[1]];
-      }
+  for (int s = 0; s < v; ++s) {
+    const uint32_t h = hu ^ tab_word<SH>(hc, hca, (uint32_t)x0);
+    const uint32_t m = bloom_bits(h, F);
+    if ((tab_word<SH>(lk.filt, fa, h & wmask) & m) == m) {
+      x[0] = x0;
+      probe_bucket<ML>(sv, lk, t, sw, h, x, k, k == 1 ? x0 : top, lb);
     }
-  } else if (k == 3) {
-    uint32_t h2 = hs ^ hc[x[2]];
-    uint32_t h1 = h2 ^ hc[x[1]];
-    for (int s = 0; s < v; ++s) {
-      probe_prefix<ML>(sv, lk, t, sw, h1 ^ hc[x[0]], x, 3, x[2], lb);
-      if (++x[0] == x[1]) {
-        x[0] = 0;
-        if (++x[1] == x[2]) {
-          x[1] = 1;
-          h2 = hs ^ hc[++x[2]];
-        }
-        h1 = h2 ^ hc[x[1]];
-      }
-    }
-  } else {
-    uint32_t h = hs;
+    if (s + 1 < v) {
+      if (x0 + 1 < xb) {
+        ++x0;
+      } else {
+        // the upper elements advance (colex successor with x0 at its top)
+        x[0] = x0;
+        colex_next(x, k, tam - 1);
+        x0 = x[0];
+        xb = x[1];
+        hu = hs;
 #pragma unroll
-    for (int e = 0; e < 5; ++e)
-      if (e < k) h ^= hc[x[e]];
-    for (int s = 0; s < v; ++s) {
-      int cl = x[0];
-#pragma unroll
-      for (int e = 0; e < 5; ++e)
-        if (e < k) cl = x[e];
-      probe_prefix<ML>(sv, lk, t, sw, h, x, k, cl, lb);
-      if (s + 1 < v) {
-        int old[5];
-#pragma unroll
-        for (int e = 0; e < 5; ++e) old[e] = x[e];
-        const int adv = colex_next(x, k, tam - 1);
-#pragma unroll
-        for (int e = 0; e < 5; ++e)
-          if (e < k && e <= adv && old[e] != x[e]) h ^= hc[old[e]] ^ hc[x[e]];
+        for (int e = 1; e < 5; ++e)
+          if (e < k) {
+            hu ^= hc[x[e]];
+            top = x[e];
+          }
       }
     }
   }
+  return lb;
 }
 
 // Lookup tiles of a weight block with nprefix prefixes.

@@ -71,6 +71,14 @@ static __device__ Winner winner_ml(const Job &J) {
   return wn;
 }
 
+// What a tile evaluation reads about its weight block and lookup tables: one
+// copy per warp in shared memory, written by lane 0 when the warp moves to
+// another block, so that none of it occupies registers between tiles.
+struct TileView {
+  SegView sv;
+  LookView lk;
+};
+
 // Per-warp state carried from one drawn tile range to the next: the last Job
 // and weight block looked up (tiles of one draw are consecutive, so the lookups
 // are mostly reused) and which iteration's lookup block is in the stage.
@@ -80,8 +88,7 @@ struct SearchCache {
   unsigned long long cj_lo, cj_hi, cs_lo, cs_hi;
   Job *Jp;
   const DevCode *cdp;
-  SegView sv;
-  LookView lk;
+  int staged;  // the lookup block is in the warp's stage
   int s_iter, s_ml, s_prob;
   __device__ void reset() {
     st_job = st_it = -1;
@@ -89,7 +96,7 @@ struct SearchCache {
     cj_lo = cj_hi = cs_lo = cs_hi = 0;
     Jp = nullptr;
     cdp = nullptr;
-    s_iter = s_ml = s_prob = 0;
+    staged = s_iter = s_ml = s_prob = 0;
   }
   // the stage was used for other work: its tables are gone
   __device__ void stage_lost() { st_job = st_it = -1; }
@@ -100,7 +107,7 @@ struct SearchCache {
 // sketches (or, while a Job is finished, the Job).
 template <bool MLK>
 __device__ void search_tiles(const DevBatch &b, unsigned long long t0, unsigned long long t1,
-                             unsigned long long njobs, WarpArea &A, SearchCache &c) {
+                             unsigned long long njobs, WarpArea &A, SearchCache &c, TileView &V) {
   const int lane = threadIdx.x & 31;
   uint32_t *stage = reinterpret_cast<uint32_t *>(&A);
   uint32_t *sw = stage + kWarpStage;
@@ -111,6 +118,7 @@ __device__ void search_tiles(const DevBatch &b, unsigned long long t0, unsigned 
   unsigned long long pending = 0;
   bool fenced = false;
   for (unsigned long long t = t0; t < t1; ++t) {
+    unsigned long long tp = b.profile ? global_ns() : 0ull;
     if (c.cj < 0 || t < c.cj_lo || t >= c.cj_hi) {
       const int lo = warp_search_le(0, (int)njobs - 1, t,
                                     [&](int j) { return b.jobs[j].tile_base; });
@@ -146,29 +154,35 @@ __device__ void search_tiles(const DevBatch &b, unsigned long long t0, unsigned 
       c.s_iter = S.iter;
       c.s_ml = MLK && c.cdp->variant == kMl;
       c.s_prob = c.cdp->variant == kProb;
-      // the iteration's lookup block (sketches, filter, buckets) is staged when
-      // it fits; the full columns stay in the Job's scratch for the exact tests
+      // the iteration's lookup block (sketches, filter, buckets) is built in
+      // the stage when it fits (otherwise the publisher built it in the
+      // scratch); the full columns stay in the Job's scratch for exact tests
       const LookLayout L = look_layout(I.tam, kWarpStage);
-      const bool staged = L.words <= kWarpStage;
-      const uint32_t *blk = staged ? stage : I.hcols;
-      c.sv = SegView{blk, I.cols, I.llr, J.hs, I.tam, S.w, kLookK, c.cdp->nwp,
-                     c.cdp->nw, S.nprefix, S.base};
-      c.lk = look_view(blk, L);
+      c.staged = L.words <= kWarpStage;
+      const uint32_t *blk = c.staged ? stage : I.hcols;
+      __syncwarp();  // every lane is done with the previous view
+      if (lane == 0) {
+        V.sv = SegView{blk, I.cols, I.llr, J.hs, I.tam, S.w, kLookK, c.cdp->nwp,
+                       c.cdp->nw, S.nprefix, S.base};
+        V.lk = look_view(blk, L);
+      }
       if (c.st_job != c.cj || c.st_it != S.iter) {
-        __syncwarp();
-        if (staged) {
+        if (c.staged) {
           const uint4 *src = reinterpret_cast<const uint4 *>(I.hcols);
           uint4 *dst = reinterpret_cast<uint4 *>(stage);
-          const int n4 = L.words / 4;
+          const int n4 = (I.tam + 3) / 4;
           for (int i = lane; i < n4; i += 32) dst[i] = __ldcg(src + i);
+          __syncwarp();
+          build_lookup(stage, I.tam, L);
         }
         sw[lane] = J.sw[lane];
-        __syncwarp();
         c.st_job = c.cj;
         c.st_it = S.iter;
       }
+      __syncwarp();
       skip_known = false;
     }
+    tp = prof_lap(b, kProfTileSetup, tp);
     if (!skip_known || c.s_ml) {
       // one decision for the warp: other warps lower the bound while lanes read it
       skip = __any_sync(kFull, tile_skip(J, J.seg[c.cs], J.it[c.s_iter], c.s_ml));
@@ -176,11 +190,15 @@ __device__ void search_tiles(const DevBatch &b, unsigned long long t0, unsigned 
     }
     bool published = false;
     if (!skip) {
-      LaneBest lb;
-      lb.reset();
       const unsigned long long st = lt - c.cs_lo;
-      if (c.s_ml) eval_lookup_tile<kLookK, true>(c.sv, c.lk, b.ncr, sw, st, lb);
-      else eval_lookup_tile<kLookK, false>(c.sv, c.lk, b.ncr, sw, st, lb);
+      LaneBest lb;
+      if (c.staged) {
+        if (MLK && c.s_ml) lb = eval_lookup_tile<kLookK, MLK, true>(V.sv, V.lk, b.ncr, sw, st);
+        else lb = eval_lookup_tile<kLookK, false, true>(V.sv, V.lk, b.ncr, sw, st);
+      } else {
+        if (MLK && c.s_ml) lb = eval_lookup_tile<kLookK, MLK, false>(V.sv, V.lk, b.ncr, sw, st);
+        else lb = eval_lookup_tile<kLookK, false, false>(V.sv, V.lk, b.ncr, sw, st);
+      }
       // a tile without a match (nearly every tile) skips the reductions
       if (!c.s_ml) {
         if (__any_sync(kFull, lb.g != kNone)) {
@@ -194,7 +212,7 @@ __device__ void search_tiles(const DevBatch &b, unsigned long long t0, unsigned 
         unsigned long long r = lb.r;
         warp_min_key(o, r);
         published = true;
-        if (lane == 0 && !atomic_min_key(J.mlkey[c.s_iter][c.sv.w], o, r))
+        if (lane == 0 && !atomic_min_key(J.mlkey[c.s_iter][J.seg[c.cs].w], o, r))
           atomicOr(b.status, kStatusCasLimit);
       }
     }
@@ -230,6 +248,7 @@ __device__ void search_tiles(const DevBatch &b, unsigned long long t0, unsigned 
         else wn = winner_ml(F);
         finish_shot(b, *c.cdp, F, F.shot, wn, F.ebits, delta);
         __syncwarp();
+        prof_lap(b, kProfTileFinish, tp);
       }
     }
   }

@@ -118,9 +118,13 @@ static __device__ int plan_next(const DevCode &cd, int tam0, int tam1, int tam2,
 // ---------------------------------------------------------------------------
 // Staging of one iteration's active set (positions, columns, sketches, LLRs).
 // ---------------------------------------------------------------------------
+// pos, tmp (unsorted ML list) and key (ML sort keys) are the warp's working
+// arrays: shared memory wherever they fit, so that the gathers below read the
+// positions without a round trip to L2.
 template <bool MLK>
 __device__ void stage_iteration(const DevCode &cd, const uint32_t *am, int tam, int *pos,
-                                int *tmp, uint32_t *cols, uint32_t *hcols, float *llr) {
+                                int *tmp, float *key, uint32_t *cols, uint32_t *hcols,
+                                float *llr) {
   const int lane = threadIdx.x & 31;
   const bool ml = MLK && cd.variant == kMl;
   int *dst = ml ? tmp : pos;
@@ -135,13 +139,16 @@ __device__ void stage_iteration(const DevCode &cd, const uint32_t *am, int tam, 
   }
   __syncwarp();
   if (ml) {
-    // stable sort by LLR ascending (upstream insertion sort, grand_decoder.cu:598-610)
+    // stable sort by LLR ascending (upstream insertion sort, grand_decoder.cu:598-610):
+    // the keys in list order first, then each element's rank among them
+    for (int i = lane; i < tam; i += 32) key[i] = __ldg(cd.llr + tmp[i]);
+    __syncwarp();
     for (int i = lane; i < tam; i += 32) {
-      const float key = __ldg(cd.llr + tmp[i]);
+      const float ki = key[i];
       int r = 0;
       for (int j = 0; j < tam; ++j) {
-        const float kj = __ldg(cd.llr + tmp[j]);
-        r += (kj < key) || (kj == key && j < i);
+        const float kj = key[j];
+        r += (kj < ki) || (kj == ki && j < i);
       }
       pos[r] = tmp[i];
     }
@@ -370,7 +377,8 @@ __device__ void light_search(const DevBatch &b, const DevCode &cd, Job &J, WarpA
   const int lane = threadIdx.x & 31;
   const bool ml = MLK && cd.variant == kMl;
   IterInfo &I = J.it[ii];
-  stage_iteration<MLK>(cd, A.am[I.src], I.tam, A.pos, A.tmp, A.cols, A.hcols, A.llr);
+  stage_iteration<MLK>(cd, A.am[I.src], I.tam, A.pos, A.tmp, reinterpret_cast<float *>(A.hcols),
+                       A.cols, A.hcols, A.llr);
   if (lane == 0) {
     I.pos = A.pos;
     I.cols = A.cols;
@@ -386,7 +394,9 @@ __device__ void light_search(const DevBatch &b, const DevCode &cd, Job &J, WarpA
     }
   }
   __syncwarp();
-  const bool small = I.tam <= kSmallTam;
+  // every subset at once only while that is not much more than the iteration's
+  // candidates (weights above W would be most of the 2^tam masks)
+  const bool small = I.tam <= kSmallTam && (1ull << I.tam) <= 4ull * I.total;
   uint32_t SO[kMaxW + 1];
   unsigned long long SR[kMaxW + 1];
   if (!ml) {
@@ -485,6 +495,7 @@ __device__ void triage_shot(const DevBatch &b, int slot, WarpArea &A, PlanState 
   const int lane = threadIdx.x & 31;
   {
     const unsigned long long t_start = global_ns();
+    unsigned long long tp = b.profile ? t_start : 0ull;
     const int shot = b.shot_map ? b.shot_map[slot] : slot;
     const int ci = b.shot_code ? b.shot_code[shot] : 0;
     const DevCode &cd = b.codes[ci];
@@ -554,6 +565,7 @@ __device__ void triage_shot(const DevBatch &b, int slot, WarpArea &A, PlanState 
     A.sw[lane] = (lane < cd.nw) ? s_lane : 0u;
     const bool empty = !__any_sync(kFull, s_lane != 0u);  // lanes >= nw hold 0
     __syncwarp();
+    tp = prof_lap(b, kProfShotPack, tp);
 
     if (empty) {  // grand_decoder.cu:1223-1241: nothing to search
       // the 72-byte result as 18 words, one per lane: original_weight (word 2)
@@ -659,6 +671,7 @@ __device__ void triage_shot(const DevBatch &b, int slot, WarpArea &A, PlanState 
       J.t_start = t_start;
       J.t_counts = global_ns();
     }
+    tp = prof_lap(b, kProfShotCounts, tp);
 
     // ---- iterations in upstream order; the first one over the light budget
     //      and everything after it go to the search kernel ---------------------
@@ -696,14 +709,17 @@ __device__ void triage_shot(const DevBatch &b, int slot, WarpArea &A, PlanState 
       }
       if (wn.found) break;
     }
+    tp = prof_lap(b, kProfShotLight, tp);
     if (heavy_from < 0) {
       finish_shot(b, cd, J, shot, wn, A.eb, A.delta);
       if (b.deferred && lane == 0) b.deferred[shot] = 0;
       __syncwarp();
+      prof_lap(b, kProfShotFinish, tp);
       return;
     }
 
     // ---- heavy: publish a Job ------------------------------------------------
+    unsigned long long tq = tp;
     syndrome_sketch();
     unsigned long long words = 0;
     for (int ii = heavy_from; ii < J.n_it; ++ii) {
@@ -719,17 +735,16 @@ __device__ void triage_shot(const DevBatch &b, int slot, WarpArea &A, PlanState 
     unsigned long long off = 0, jslot = 0, tbase = 0, ntl = 0;
     int ok = 1;
     if (lane == 0) {
-      // A reservation that does not fit takes nothing, so one oversized shot
-      // does not make the shots after it fail too (they are re-run otherwise).
+      // One atomicAdd, after a check that the reservation fits what is left: a
+      // shot larger than that touches nothing, so it does not make the shots
+      // after it fail too, and the first reservation of a launch that fits the
+      // arena always succeeds.  Reservations racing for the last words may all
+      // overshoot; those shots are re-run like any other that did not fit.
       ok = 0;
       off = *reinterpret_cast<volatile unsigned long long *>(ctr_ptr(b.counters, kCtrScratchTop));
-      for (int guard = 0; guard < (1 << 16) && off + words <= b.scratch_words; ++guard) {
-        const unsigned long long seen = atomicCAS(ctr_ptr(b.counters, kCtrScratchTop), off, off + words);
-        if (seen == off) {
-          ok = 1;
-          break;
-        }
-        off = seen;
+      if (off + words <= b.scratch_words) {
+        off = atomicAdd(ctr_ptr(b.counters, kCtrScratchTop), words);
+        ok = off + words <= b.scratch_words ? 1 : 0;
       }
       if (!ok) atomicOr(b.status, kStatusScratchOverflow);
     }
@@ -740,6 +755,7 @@ __device__ void triage_shot(const DevBatch &b, int slot, WarpArea &A, PlanState 
       return;
     }
     off = __shfl_sync(kFull, off, 0);
+    tq = prof_lap(b, kProfPubReserve, tq, kCtrProfMore);
     uint32_t *sp = b.scratch + off;
     for (int ii = heavy_from; ii < J.n_it; ++ii) {
       IterInfo &I = J.it[ii];
@@ -757,9 +773,20 @@ __device__ void triage_shot(const DevBatch &b, int slot, WarpArea &A, PlanState 
         llr = reinterpret_cast<float *>(sp);
         sp += (tm + 3ull) & ~3ull;
       }
-      stage_iteration<MLK>(cd, A.am[I.src], I.tam, pos, tmp, cols, hcols, llr);
-      // the light search's arrays are free now: the table builder's scratch
-      build_lookup(hcols, I.tam, LL, A.cols);
+      // positions (and the ML sort) in the light search's arrays, which are
+      // free now, when they fit; then copied to the scratch
+      const bool sh = (ml ? 3 : 1) * I.tam <= kPublishWords;
+      int *wpos = sh ? reinterpret_cast<int *>(A.cols) : pos;
+      int *wtmp = sh ? wpos + I.tam : tmp;
+      float *wkey = sh ? reinterpret_cast<float *>(wpos + 2 * I.tam) : reinterpret_cast<float *>(hcols);
+      stage_iteration<MLK>(cd, A.am[I.src], I.tam, wpos, wtmp, wkey, cols, hcols, llr);
+      if (sh) {
+        for (int i = lane; i < I.tam; i += 32) pos[i] = wpos[i];
+        __syncwarp();
+      }
+      // an active set too large for a search warp's stage: its tables are
+      // built here, once, in the scratch
+      if (LL.words > kWarpStage) build_lookup(hcols, I.tam, LL);
       if (lane == 0) {
         I.pos = pos;
         I.cols = cols;
@@ -776,6 +803,7 @@ __device__ void triage_shot(const DevBatch &b, int slot, WarpArea &A, PlanState 
       }
       __syncwarp();
     }
+    tq = prof_lap(b, kProfPubStage, tq, kCtrProfMore);
     if (lane == 0) {
       J.it_lo = heavy_from;
       for (int sgi = 0; sgi < J.nseg; ++sgi) {
@@ -784,18 +812,13 @@ __device__ void triage_shot(const DevBatch &b, int slot, WarpArea &A, PlanState 
         S.tile_lo = ntl;
         ntl += S.njt;
       }
-      // A Job slot and the next ntl tiles (the job table permitting); a
-      // reservation that does not fit takes nothing.
+      // A Job slot and the next ntl tiles (the job table permitting), by one
+      // atomicAdd as for the scratch above.
       ok = 0;
       unsigned long long old = ld_ctr(b, kCtrJobs);
-      for (int guard = 0; guard < (1 << 16) && (old >> 40) < (unsigned long long)b.max_jobs;
-           ++guard) {
-        const unsigned long long seen = atomicCAS(ctr_ptr(b.counters, kCtrJobs), old, old + (1ull << 40) + ntl);
-        if (seen == old) {
-          ok = 1;
-          break;
-        }
-        old = seen;
+      if ((old >> 40) < (unsigned long long)b.max_jobs) {
+        old = atomicAdd(ctr_ptr(b.counters, kCtrJobs), (1ull << 40) + ntl);
+        ok = (old >> 40) < (unsigned long long)b.max_jobs ? 1 : 0;
       }
       if (!ok) atomicOr(b.status, kStatusJobOverflow);
       jslot = old >> 40;
@@ -827,6 +850,7 @@ __device__ void triage_shot(const DevBatch &b, int slot, WarpArea &A, PlanState 
       for (int i = lane; i < (int)(sizeof(Job) / 4); i += 32) dst[i] = src[i];
     }
     if (lane == 0 && b.deferred) b.deferred[shot] = 0;
+    tq = prof_lap(b, kProfPubWrite, tq, kCtrProfMore);
     // The Job is searchable once its ready word holds this launch's tag: each
     // lane orders its part of the copy (and the staged scratch) before it.
     __threadfence();
@@ -835,9 +859,11 @@ __device__ void triage_shot(const DevBatch &b, int slot, WarpArea &A, PlanState 
       __threadfence();
       *reinterpret_cast<volatile unsigned *>(&b.jobs[jslot].ready) = tag;
       __threadfence();
-      advance_front(b, tag);
     }
     __syncwarp();
+    advance_front(b, tag);
+    prof_lap(b, kProfPubReady, tq, kCtrProfMore);
+    prof_lap(b, kProfShotPublish, tp);
   }
 }
 
@@ -931,6 +957,7 @@ __device__ void classify_chunk(const DevBatch &b, int chunk, WarpArea &A, unsign
   const int slot = chunk * 32 + lane;
   const bool valid = slot < b.num_shots;
   const unsigned long long t_start = global_ns();
+  unsigned long long tp = b.profile ? t_start : 0ull;
   const int shot = valid ? (b.shot_map ? b.shot_map[slot] : slot) : 0;
   const int ci = (valid && b.shot_code) ? b.shot_code[shot] : 0;
   const DevCode &cd = b.codes[ci];
@@ -1057,6 +1084,7 @@ __device__ void classify_chunk(const DevBatch &b, int chunk, WarpArea &A, unsign
     }
   }
   if (!errs) ow = 0;
+  tp = prof_lap(b, kProfChunkRead, tp);
 
   // ---- settle: empty syndrome, or a one-position first iteration matched ----
   const bool empty = ok && (s[0] | s[1] | s[2] | s[3]) == 0u;
@@ -1108,6 +1136,7 @@ __device__ void classify_chunk(const DevBatch &b, int chunk, WarpArea &A, unsign
   }
   const bool done = empty || found;
   if (!found) pos = -1;
+  tp = prof_lap(b, kProfChunkTest, tp);
 
   // ---- results of the settled shots ----------------------------------------
   if (done) {
@@ -1180,6 +1209,7 @@ __device__ void classify_chunk(const DevBatch &b, int chunk, WarpArea &A, unsign
           ((unsigned long long)tag << 32) | (unsigned)slot;
   }
   __syncwarp();
+  prof_lap(b, kProfChunkWrite, tp);
 }
 
 }  // namespace grand

@@ -157,9 +157,24 @@ class Engine:
     def launch_stats(self, stream=0):
         """(settled by classification, per-shot path, Jobs, tiles, scratch words) of the
         last device decode on `stream`."""
-        out = (ctypes.c_longlong * 5)()
+        out = (ctypes.c_longlong * 28)()
         rc = self.lib.grand_engine_launch_stats(self.h, stream or None, out)
-        return tuple(out) if rc == 0 else None
+        return tuple(out[:5]) if rc == 0 else None
+
+    def launch_profile(self, stream=0):
+        """Phase profile of the last device decode on `stream` (the engine created
+        with GRAND_PROFILE=1): warp-ns per kind of work, when the last of each kind
+        ended (ns after the first warp started) and the number of work steps."""
+        out = (ctypes.c_longlong * 28)()
+        rc = self.lib.grand_engine_launch_stats(self.h, stream or None, out)
+        if rc != 0:
+            return None
+        kinds = ("chunks", "shots", "tiles", "wait")
+        parts = ("chunk_read", "chunk_test", "chunk_write", "shot_pack", "shot_counts",
+                 "shot_light", "shot_publish", "shot_finish", "tile_setup", "tile_finish")
+        return {"warp_ns": dict(zip(kinds, out[5:9])), "last_end_ns": dict(zip(kinds, out[9:13])),
+                "steps": out[13], "split_warp_ns": dict(zip(parts, out[14:24])),
+                "publish_warp_ns": dict(zip(("reserve", "stage", "write", "ready"), out[24:28]))}
 
     def batch_times(self):
         """(h2d, triage, search, d2h) ms of the last host-buffer decode."""

@@ -194,6 +194,13 @@ static inline unsigned long long atomicMin(unsigned long long *a, unsigned long 
   }
   return cur;
 }
+static inline unsigned long long atomicMax(unsigned long long *a, unsigned long long v) {
+  unsigned long long cur = __atomic_load_n(a, __ATOMIC_SEQ_CST);
+  while (v > cur &&
+         !__atomic_compare_exchange_n(a, &cur, v, false, __ATOMIC_SEQ_CST, __ATOMIC_SEQ_CST)) {
+  }
+  return cur;
+}
 static inline unsigned atomicCAS(unsigned *a, unsigned cmp, unsigned v) {
   __atomic_compare_exchange_n(a, &cmp, v, false, __ATOMIC_SEQ_CST, __ATOMIC_SEQ_CST);
   return cmp;
@@ -222,6 +229,9 @@ static inline void grand_host_cas128(unsigned long long *slot, unsigned long lon
 #define __shared__ static
 #ifndef __launch_bounds__
 #define __launch_bounds__(...)
+#endif
+#ifndef __noinline__
+#define __noinline__ __attribute__((noinline))
 #endif
 
 #define GRAND_HOST_EMULATION 1
