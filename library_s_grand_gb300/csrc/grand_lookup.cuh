@@ -204,13 +204,117 @@ __device__ __forceinline__ void probe_bucket(const SegView &sv, const LookView &
   }
 }
 
+// Colex walk over the prefixes of one lane, for prefixes of KP elements
+// (KP = 0: the runtime k, any length): x0 (the lowest element) rises under the
+// upper elements x[1..k-1], whose sketch XOR h(s) is hu; when x0 meets x1 the
+// upper elements take their colex successor.  For KP = 1..4 the carry is a few
+// increments with the partial sketches kept (hp[e] = h(s) ^ hc[x_e] ^ .. ^
+// hc[x_{k-1}]), so a lane that carries (while the others wait) costs little.
+template <int KP>
+struct PrefixWalk {
+  int x[5];
+  uint32_t hp[5];
+  int k, tam;
+  uint32_t hs;
+  __device__ __forceinline__ int kk() const { return KP ? KP : k; }
+  template <bool SH>
+  __device__ __forceinline__ void start(const unsigned long long *t, unsigned long long q, int k_,
+                                        int tam_, uint32_t hs_, const uint32_t *hc, uint32_t hca) {
+    k = k_;
+    tam = tam_;
+    hs = hs_;
+#pragma unroll
+    for (int e = 0; e < 5; ++e) x[e] = e;
+    sub_unrank(t, q, kk(), tam - 1, x);
+    sketches<SH>(4, hc, hca);
+  }
+  // hp[e] for the upper elements from position e0 down to 1
+  template <bool SH>
+  __device__ __forceinline__ void sketches(int e0, const uint32_t *hc, uint32_t hca) {
+    uint32_t h = hs;
+#pragma unroll
+    for (int e = 4; e >= 1; --e) {
+      if (e < kk()) {
+        if (e <= e0) hp[e] = (e + 1 < kk() ? hp[e < 4 ? e + 1 : 4] : hs) ^
+                             tab_word<SH>(hc, hca, (uint32_t)x[e]);
+        h = hp[e];
+      }
+    }
+    hp[0] = kk() >= 2 ? h : hs;
+  }
+  __device__ __forceinline__ uint32_t hu() const { return hp[0]; }
+  __device__ __forceinline__ int top() const {
+    int t0 = x[0];
+#pragma unroll
+    for (int e = 1; e < 5; ++e)
+      if (e < kk()) t0 = x[e];
+    return t0;
+  }
+  template <bool SH>
+  __device__ __forceinline__ void next(const uint32_t *hc, uint32_t hca) {
+    const int k1 = kk();
+    if (k1 == 1) {
+      ++x[0];
+      return;
+    }
+    if (x[0] + 1 < x[1]) {
+      ++x[0];
+      return;
+    }
+    // carry: the lowest upper element with room rises, those below restart
+    int e = 1;
+#pragma unroll
+    for (int i = 1; i < 5; ++i)
+      if (i < k1 && e == i && x[i] + 1 == (i + 1 < k1 ? x[i < 4 ? i + 1 : 4] : tam - 1)) e = i + 1;
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+      if (i < e) x[i] = i;
+      else if (i == e) ++x[i];
+    }
+    sketches<SH>(e, hc, hca);
+  }
+};
+
+// The scan of one lane's v prefixes starting at colex rank q (KP: prefix length,
+// 0 = runtime).  Per prefix: its sketch hu ^ hc[x0] (one staged load), one
+// filter load and a three-bit test, whose outcome is only ORed into a flag:
+// the scan has no data-dependent branch but the carry into the upper elements,
+// so the loads of consecutive prefixes overlap.  A lane whose flag is set
+// (rare) walks its prefixes again and looks each filter hit up in the buckets.
+template <int KP, int K, bool ML, bool SH>
+__device__ __forceinline__ void scan_lane(const SegView &sv, const LookView &lk,
+                                          const unsigned long long *t, const uint32_t *sw,
+                                          unsigned long long q, int v, LaneBest &lb) {
+  const int k = sv.w - 1;
+  const uint32_t *hc = sv.hcols;
+  const uint32_t hca = SH ? smem_addr(hc) : 0u, fa = SH ? smem_addr(lk.filt) : 0u;
+  const uint32_t wmask = lk.wmask;
+  const int F = lk.F;
+  PrefixWalk<KP> pw;
+  pw.template start<SH>(t, q, k, sv.tam, sv.hs, hc, hca);
+  unsigned flag = 0u;
+#pragma unroll 4
+  for (int s = 0; s < K; ++s) {
+    const uint32_t h = pw.hu() ^ tab_word<SH>(hc, hca, (uint32_t)pw.x[0]);
+    const uint32_t m = bloom_bits(h, F);
+    flag |= ((tab_word<SH>(lk.filt, fa, h & wmask) & m) == m && s < v) ? 1u : 0u;
+    if (s + 1 < v) pw.template next<SH>(hc, hca);
+  }
+  if (flag) {
+    pw.template start<SH>(t, q, k, sv.tam, sv.hs, hc, hca);
+    for (int s = 0; s < v; ++s) {
+      const uint32_t h = pw.hu() ^ tab_word<SH>(hc, hca, (uint32_t)pw.x[0]);
+      const uint32_t m = bloom_bits(h, F);
+      if ((tab_word<SH>(lk.filt, fa, h & wmask) & m) == m)
+        probe_bucket<ML>(sv, lk, t, sw, h, pw.x, k, pw.top(), lb);
+      if (s + 1 < v) pw.template next<SH>(hc, hca);
+    }
+  }
+}
+
 // One lookup tile: lane l takes the K colex-consecutive prefixes
 // tile * 32K + l * K + [0, K) of the block's C(tam - 1, w - 1) prefixes (ascending
-// (w-1)-subsets of [0, tam - 1), so each has at least one j above it).  The
-// prefix sketch is the upper elements' sketch hu = h(s) ^ hc[x1] ^ ... (kept in
-// a register) XOR hc[x0]: a colex step raises x0, and only when x0 meets x1 do
-// the upper elements advance (hu recomputed).  Per prefix: one staged sketch
-// load, one filter load and a three-bit test; a filter hit walks its bucket.
+// (w-1)-subsets of [0, tam - 1), so each has at least one j above it).
 // SH: the tables are in the warp's stage (explicit shared-memory loads).  Not
 // inlined: the scan gets the whole register budget instead of sharing it with
 // the scheduling state of the persistent kernel around it (sv and lk are the
@@ -223,58 +327,23 @@ __device__ __noinline__ LaneBest eval_lookup_tile(const SegView &sv, const LookV
   lb.reset();
   const int lane = threadIdx.x & 31;
   const int k = sv.w - 1;
-  const int tam = sv.tam;
-  const uint32_t *hc = sv.hcols;
-  const uint32_t hca = SH ? smem_addr(hc) : 0u, fa = SH ? smem_addr(lk.filt) : 0u;
-  const uint32_t wmask = lk.wmask;
-  const int F = lk.F;
-  const uint32_t hs = sv.hs;
   const unsigned long long q = tile * (32ull * K) + (unsigned long long)lane * K;
   if (q >= sv.nprefix) return lb;
   const int v = (sv.nprefix - q) < (unsigned long long)K ? (int)(sv.nprefix - q) : K;
-  int x[5] = {0, 1, 2, 3, 4};
   if (k == 0) {  // weight 1: the empty prefix, every j
-    const uint32_t m = bloom_bits(hs, F);
-    if ((tab_word<SH>(lk.filt, fa, hs & wmask) & m) == m)
-      probe_bucket<ML>(sv, lk, t, sw, hs, x, 0, -1, lb);
+    const int x[5] = {0, 1, 2, 3, 4};
+    const uint32_t m = bloom_bits(sv.hs, lk.F);
+    const uint32_t fw = SH ? tab_word<SH>(lk.filt, smem_addr(lk.filt), sv.hs & lk.wmask)
+                           : lk.filt[sv.hs & lk.wmask];
+    if ((fw & m) == m) probe_bucket<ML>(sv, lk, t, sw, sv.hs, x, 0, -1, lb);
     return lb;
   }
-  sub_unrank(t, q, k, tam - 1, x);
-  int x0 = x[0];
-  int xb = k >= 2 ? x[1] : tam - 1;  // x0 stays below this until the upper part moves
-  int top = x[0];                    // the largest element (k >= 2)
-  uint32_t hu = hs;
-#pragma unroll
-  for (int e = 1; e < 5; ++e)
-    if (e < k) {
-      hu ^= hc[x[e]];
-      top = x[e];
-    }
-  for (int s = 0; s < v; ++s) {
-    const uint32_t h = hu ^ tab_word<SH>(hc, hca, (uint32_t)x0);
-    const uint32_t m = bloom_bits(h, F);
-    if ((tab_word<SH>(lk.filt, fa, h & wmask) & m) == m) {
-      x[0] = x0;
-      probe_bucket<ML>(sv, lk, t, sw, h, x, k, k == 1 ? x0 : top, lb);
-    }
-    if (s + 1 < v) {
-      if (x0 + 1 < xb) {
-        ++x0;
-      } else {
-        // the upper elements advance (colex successor with x0 at its top)
-        x[0] = x0;
-        colex_next(x, k, tam - 1);
-        x0 = x[0];
-        xb = x[1];
-        hu = hs;
-#pragma unroll
-        for (int e = 1; e < 5; ++e)
-          if (e < k) {
-            hu ^= hc[x[e]];
-            top = x[e];
-          }
-      }
-    }
+  switch (k) {
+    case 1: scan_lane<1, K, ML, SH>(sv, lk, t, sw, q, v, lb); break;
+    case 2: scan_lane<2, K, ML, SH>(sv, lk, t, sw, q, v, lb); break;
+    case 3: scan_lane<3, K, ML, SH>(sv, lk, t, sw, q, v, lb); break;
+    case 4: scan_lane<4, K, ML, SH>(sv, lk, t, sw, q, v, lb); break;
+    default: scan_lane<0, K, ML, SH>(sv, lk, t, sw, q, v, lb); break;
   }
   return lb;
 }
