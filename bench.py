@@ -14,9 +14,10 @@ Reported (one JSON line, rank 0):
   e2e        shots/s through the upstream-compatible C ABI (grand_decode_prob_cc)
              from host buffers, copies included;
   roofline   the decode kernel on the stress input the integer roofline is
-             defined on (random syndromes, W = 4, exhaustive enumeration), ops
-             counted as ceil(R/32)+1 per candidate (the fixed (w+1)*ceil(R/32)
-             count is reported beside it), against the measured lop3 issue rate;
+             defined on (random syndromes, W = 4, exhaustive enumeration):
+             candidates at 1.5 integer ops each against the measured lop3 issue
+             rate, and beside it the prefix probes the lookup search executes
+             against the shared-memory bound of two words per probe;
   cpu_baseline  the upstream CPU search algorithm (its C restatement in oracle/,
              or the upstream library itself where it was built) on all host cores.
 
@@ -217,14 +218,16 @@ class Clocks:
 # GPU arm
 # ---------------------------------------------------------------------------
 def stress_ops(code_h, syndromes, W):
-    """Exhaustive search work of random-syndrome shots: (candidates, ops) with
-    ops = (w+1)*ceil(R/32) per weight-w candidate, iteration sets as upstream."""
+    """Exhaustive search work of random-syndrome shots, iteration sets as upstream:
+    (candidates, ops, prefixes) with ops = (w+1)*ceil(R/32) per weight-w
+    candidate and prefixes = the C(tam-1, w-1) (w-1)-prefixes a weight-w block
+    is split into (one probe each in the lookup search)."""
     R = code_h.shape[0]
     words = math.ceil(R / 32)
     colw = code_h.sum(axis=0)
     max_soma = int(colw.max())
     sums = syndromes.astype(np.int64) @ code_h.astype(np.int64)
-    cands = ops = 0
+    cands = ops = prefixes = 0
     for s in sums:
         for it in range(min(max_soma, 3)):
             tam = int((s >= max_soma - it).sum())
@@ -232,7 +235,8 @@ def stress_ops(code_h, syndromes, W):
                 c = math.comb(tam, w)
                 cands += c
                 ops += c * (w + 1) * words
-    return cands, ops
+                prefixes += math.comb(tam - 1, w - 1) if tam >= w else 0
+    return cands, ops, prefixes
 
 
 def run_ours(args):
@@ -405,9 +409,9 @@ def run_ours(args):
     return out
 
 
-# DRAM bytes (read + write) of one triage_kernel launch on the headline batch, from an ncu
-# --set full capture of `bench.py --case headline`.
-TRIAGE_TRAFFIC = 9.541120e6 + 0.0
+# DRAM bytes (read + write) of one decode_kernel launch on the headline batch, from an ncu
+# --set full capture (profiles/decode_kernel_prob_cc_bb144_16384.md).
+TRIAGE_TRAFFIC = 9.659904e6 + 768.0
 
 
 def hbm_peak():
@@ -435,9 +439,14 @@ def hbm_streaming(code, dec_ms):
 
 STRESS_SHOTS = 192
 SKETCH_OPS_PER_CANDIDATE = 1.5
-# DRAM bytes (read + write) of one search_kernel launch on the stress input, from an ncu
-# --set full capture of `bench.py --case stress` (48 shots), scaled to 192 shots.
-STRESS_TRAFFIC_PER_SHOT = (1.940992e6 + 6.144e3) / 48
+# DRAM bytes (read + write) of one decode_kernel launch on the 192 stress shots, from an
+# ncu --set full capture (profiles/decode_kernel_stress_bb144_w4.md), per shot.
+STRESS_TRAFFIC_PER_SHOT = (289024.0 + 7936.0) / 192
+# The lookup search's bound per prefix probe: two shared-memory words (the last
+# element's sketch and one filter word) at 32 words per SM per clock.
+PROBE_WORDS = 2
+SMEM_WORDS_PER_SM_CLOCK = 32
+SM_CLOCK_HZ = 2.07e9  # the GB300's maximum SM clock (the runs' median clock, bench `clocks`)
 
 
 def stress_case(torch, lib, dev, n=STRESS_SHOTS):
@@ -454,19 +463,22 @@ def stress_case(torch, lib, dev, n=STRESS_SHOTS):
 
 
 def stress_roofline(torch, lib, dev, sp):
-    """Search kernel on exhaustive random-syndrome shots of [[144,12,12]], W=4.
+    """Decode kernel on exhaustive random-syndrome shots of [[144,12,12]], W=4.
 
-    Convention: the search tests a 32-bit GF(2)-linear sketch of every candidate,
-    so a candidate needs one XOR (its last column's sketch against the prefix
-    sketch) and half a 3-way minimum: 1.5 integer ops, whatever R; the peak is
-    the lop3 issue rate measured on this GPU.  Two wider conventions are reported
-    beside it: the word-compare count ceil(R/32)+1 (XOR-OR over every word of the
-    prefix-reduced target plus a minimum; 4 for R = 72) and the fixed count
-    (w+1)*ceil(R/32), which charges the full XOR of w columns to every candidate."""
+    Candidate convention (comparable across versions of the search): a candidate
+    tested by a sketch scan costs one XOR (its last column's sketch against the
+    prefix sketch) and half a 3-way minimum, 1.5 integer ops whatever R, against
+    the lop3 issue rate measured on this GPU; the word-compare count ceil(R/32)+1
+    and the fixed count (w+1)*ceil(R/32) are reported beside it.  The lookup
+    search tests a prefix's candidates with one probe, so it also gets a probe
+    convention: prefix probes per second against the shared-memory bound of two
+    words per probe (the fraction of the machine the search itself uses)."""
     from library_s_grand_gb300 import capi
     n = STRESS_SHOTS
     code, syn, eng, d_rec, d_res = stress_case(torch, lib, dev, n)
-    cands, ops_fixed = stress_ops(code.hz, syn, 4)
+    cands, ops_fixed, prefixes = stress_ops(code.hz, syn, 4)
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    probe_peak = sms * SMEM_WORDS_PER_SM_CLOCK / PROBE_WORDS * SM_CLOCK_HZ
     words = math.ceil(code.n / 32)
     times = []
     for rep in range(4):
@@ -493,7 +505,12 @@ def stress_roofline(torch, lib, dev, sp):
             "word_convention": f"ceil(R/32)+1 = {words + 1} ops per candidate (XOR-OR words + min)",
             "frac_fixed_convention": ops_fixed / (search_ms * 1e-3) / peak,
             "fixed_convention": "(w+1)*ceil(R/32) ops per candidate",
-            "peak_source": "lop3.b32 issue rate measured on this GPU (grand_measure_int_peak)"}
+            "peak_source": "lop3.b32 issue rate measured on this GPU (grand_measure_int_peak)",
+            "prefix_probes": prefixes, "probes_per_s": prefixes / (search_ms * 1e-3),
+            "probe_peak_per_s": probe_peak,
+            "frac_probe_convention": prefixes / (search_ms * 1e-3) / probe_peak,
+            "probe_convention": "one prefix probe = 2 shared-memory words (sketch, filter word); "
+                                "peak = SMs x 32 words/clock / 2 x 2.07 GHz"}
 
 
 def _time_device(torch, eng, n, d_rec, d_res, sp, flush, steps, warmup, d_sc=0, d_off=0):

@@ -146,8 +146,9 @@ struct DevCode {
   const float *llr;          // m
   const uint32_t *hcol;      // m column sketches
   int binary;                // every entry of H is 0 or 1 (column weights are popcounts)
-  const int *lowstart;       // R + 1: columns grouped by their lowest set row r are
-  const int *lowcols;        //   lowcols[lowstart[r] .. lowstart[r+1]) (nullptr: no groups)
+  const uint32_t *solo_keys; // solo columns (nonzero, containing no other nonzero column)
+  const int *solo_cols;      //   by sketch: open addressing, column -1 = empty slot
+  uint32_t solo_mask;        //   (solo_cols nullptr: no table)
 };
 
 // One searched weight block of one threshold iteration.

@@ -1,5 +1,6 @@
 // grand_host.cpp -- device context, code tables, workspaces and the batch driver.
 #include "grand_host.h"
+#include "grand_solo.h"
 
 #include <stdarg.h>
 #include <stdio.h>
@@ -73,8 +74,8 @@ CodeTables::~CodeTables() {
   cudaFree(pivrow);
   cudaFree(lcols);
   cudaFree(hcol);
-  cudaFree(lowstart);
-  cudaFree(lowcols);
+  cudaFree(solo_keys);
+  cudaFree(solo_cols);
 }
 
 Workspace::~Workspace() {
@@ -287,22 +288,14 @@ std::shared_ptr<CodeTables> Context::tables(int family, const int *H, const int 
       if (v != 0 && v != 1) t->binary = 0;
     }
   }
-  // nonzero columns grouped by their lowest row (ascending within a group)
-  std::vector<int> lowstart(n + 1, 0), lowcols;
-  for (int c = 0; c < m; ++c)
-    if (lowrow[c] >= 0) ++lowstart[lowrow[c] + 1];
-  for (int r = 0; r < n; ++r) lowstart[r + 1] += lowstart[r];
-  lowcols.assign(lowstart[n], 0);
-  {
-    std::vector<int> fill(lowstart.begin(), lowstart.end() - 1);
-    for (int c = 0; c < m; ++c)
-      if (lowrow[c] >= 0) lowcols[fill[lowrow[c]]++] = c;
-  }
+  // solo columns (nonzero, containing no other nonzero column) by sketch
+  const SoloTable solo = build_solo_table(cols, t->nwp, t->nw, m, hcol);
+  t->solo_mask = solo.mask;
   cudaError_t e = upload(&t->cols, cols);
   if (e == cudaSuccess) e = upload(&t->colw, colw);
   if (e == cudaSuccess) e = upload(&t->hcol, hcol);
-  if (e == cudaSuccess) e = upload(&t->lowstart, lowstart);
-  if (e == cudaSuccess) e = upload(&t->lowcols, lowcols);
+  if (e == cudaSuccess) e = upload(&t->solo_keys, solo.keys);
+  if (e == cudaSuccess) e = upload(&t->solo_cols, solo.cols);
   if (e == cudaSuccess && family == kCss) {
     std::vector<uint32_t> rows((size_t)n * t->mw, 0u);
     for (int r = 0; r < n; ++r)
@@ -376,8 +369,9 @@ DevCode make_devcode(const CodeTables &t, const CallParams &p) {
   d.llr = p.d_llr;
   d.hcol = t.hcol;
   d.binary = t.binary;
-  d.lowstart = t.lowstart;
-  d.lowcols = t.lowcols;
+  d.solo_keys = t.solo_keys;
+  d.solo_cols = t.solo_cols;
+  d.solo_mask = t.solo_mask;
   return d;
 }
 

@@ -35,8 +35,9 @@ struct CodeTables {
   uint32_t *lcols = nullptr;
   uint32_t *hcol = nullptr;  // column sketches (row_hash XOR over each column's rows)
   int binary = 1;             // every entry is 0 or 1
-  int *lowstart = nullptr;    // R + 1: nonzero columns grouped by their lowest row
-  int *lowcols = nullptr;
+  uint32_t *solo_keys = nullptr;  // solo-column table (grand_solo.h): sketches
+  int *solo_cols = nullptr;        //   and columns per slot (-1: empty)
+  uint32_t solo_mask = 0;
   std::vector<int> key;  // exact content the tables were built from
   size_t bytes = 0;
   ~CodeTables();

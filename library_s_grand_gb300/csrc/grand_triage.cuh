@@ -1090,36 +1090,31 @@ __device__ void classify_chunk(const DevBatch &b, int chunk, WarpArea &A, unsign
   const bool empty = ok && (s[0] | s[1] | s[2] | s[3]) == 0u;
   bool found = false, gpu = false;
   int pos = -1, deg = 0, iseq = 0;
-  if (ok && !empty && cd.variant != kMl && cd.lowstart && cd.binary && cd.max_soma >= 1 &&
+  if (ok && !empty && cd.variant != kMl && cd.solo_cols && cd.binary && cd.max_soma >= 1 &&
       one_position_searched(cd, &gpu)) {
-    // the first iteration's active set: nonzero columns contained in s, each
-    // reached once through its lowest row (which s must contain)
-    int tam0 = 0;
+    // the first iteration's active set is the nonzero columns contained in s:
+    // it is one column whose only candidate matches exactly when s equals a
+    // solo column, found by s's sketch in the solo table
+    uint32_t hs = 0u;
 #pragma unroll
-    for (int q = 0; q < kFastWords; ++q) {
-      uint32_t rows = q < cd.nw ? s[q] : 0u;
-      while (rows && tam0 < 2) {
-        const int r = q * 32 + __ffs(rows) - 1;
-        rows &= rows - 1u;
-        const int i1 = __ldg(cd.lowstart + r + 1);
-        for (int i = __ldg(cd.lowstart + r); i < i1 && tam0 < 2; ++i) {
-          const int c = __ldg(cd.lowcols + i);
-          bool inside = true;
+    for (int q = 0; q < kFastWords; ++q)
+      for (uint32_t rows = q < cd.nw ? s[q] : 0u; rows; rows &= rows - 1u)
+        hs ^= row_hash(q * 32 + __ffs(rows) - 1);
+    uint32_t i = hs & cd.solo_mask;
+    for (uint32_t probe = 0; probe <= cd.solo_mask && !found; ++probe) {
+      const int c = __ldg(cd.solo_cols + i);
+      if (c < 0) break;
+      if (__ldg(cd.solo_keys + i) == hs) {
+        bool eq = true;
 #pragma unroll
-          for (int k = 0; k < kFastWords; ++k)
-            if (k < cd.nw) inside = inside && (__ldg(cd.cols + (size_t)c * cd.nwp + k) & ~s[k]) == 0u;
-          if (inside) {
-            ++tam0;
-            pos = c;
-          }
+        for (int k = 0; k < kFastWords; ++k)
+          if (k < cd.nw) eq = eq && __ldg(cd.cols + (size_t)c * cd.nwp + k) == s[k];
+        if (eq) {
+          found = true;
+          pos = c;
         }
       }
-    }
-    if (tam0 == 1) {
-      found = true;
-#pragma unroll
-      for (int k = 0; k < kFastWords; ++k)
-        if (k < cd.nw) found = found && __ldg(cd.cols + (size_t)pos * cd.nwp + k) == s[k];
+      i = (i + 1u) & cd.solo_mask;
     }
     if (found) {
       if (!dem && errs) {

@@ -236,6 +236,7 @@ static inline void grand_host_cas128(unsigned long long *slot, unsigned long lon
 
 #define GRAND_HOST_EMULATION 1
 #include "grand_decode.cuh"
+#include "grand_solo.h"
 
 using namespace grand;
 
@@ -277,7 +278,8 @@ struct Code {
   int family = 0, variant = 0, input_kind = 0, n = 0, m = 0, N = 0, W = 0, nl = 0, packed = 0;
   int light = 12, tile_k = 4, rec_len = 0, log_len = 0;
   std::vector<uint32_t> cols, hcol, rows, lcols;
-  std::vector<int> colw, pivrow, lowstart, lowcols;
+  std::vector<int> colw, pivrow;
+  SoloTable solo;
   std::vector<float> llr;
   DevCode d;
 };
@@ -327,21 +329,8 @@ static bool load_code(const std::string &dir, Code &k) {
         k.cols[(size_t)c * nwp + (r >> 5)] |= 1u << (r & 31);
         k.hcol[c] ^= row_hash(r);
       }
-  // nonzero columns grouped by their lowest row, as the library builds them
-  std::vector<int> lowrow(m, -1);
-  for (int r = n - 1; r >= 0; --r)
-    for (int c = 0; c < m; ++c)
-      if (H[(size_t)r * m + c] != 0) lowrow[c] = r;
-  k.lowstart.assign(n + 1, 0);
-  for (int c = 0; c < m; ++c)
-    if (lowrow[c] >= 0) ++k.lowstart[lowrow[c] + 1];
-  for (int r = 0; r < n; ++r) k.lowstart[r + 1] += k.lowstart[r];
-  k.lowcols.assign(std::max(k.lowstart[n], 1), 0);
-  {
-    std::vector<int> fill(k.lowstart.begin(), k.lowstart.end() - 1);
-    for (int c = 0; c < m; ++c)
-      if (lowrow[c] >= 0) k.lowcols[fill[lowrow[c]]++] = c;
-  }
+  // the solo-column table, as the library builds it
+  k.solo = build_solo_table(k.cols, nwp, nw, m, k.hcol);
   int binary = 1;
   for (size_t i = 0; i < H.size(); ++i)
     if (H[i] != 0 && H[i] != 1) binary = 0;
@@ -406,8 +395,9 @@ static bool load_code(const std::string &dir, Code &k) {
   d.pivrow = k.pivrow.data();
   d.hcol = k.hcol.data();
   d.binary = binary;
-  d.lowstart = k.lowstart.data();
-  d.lowcols = k.lowcols.data();
+  d.solo_keys = k.solo.keys.data();
+  d.solo_cols = k.solo.cols.data();
+  d.solo_mask = k.solo.mask;
   return true;
 }
 
