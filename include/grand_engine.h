@@ -120,7 +120,9 @@ int grand_engine_kernel_times(GrandEngine *engine, void *stream, float *reset_ms
  * staging and publication, result written) and search (Job and block lookup
  * with staging, completed Jobs' results) and out[24..27] the Job publications
  * split into reservations, staging, the Job written and the steps that make it
- * searchable; otherwise those entries are 0 / -1.  `out` holds 28 entries. */
+ * searchable, out[28] when the last per-shot-path shot started, out[29] the
+ * longest per-shot-path shot and out[30] the longest tile draw (ns); otherwise
+ * those entries are 0 / -1.  `out` holds 31 entries. */
 int grand_engine_launch_stats(GrandEngine *engine, void *stream, long long *out);
 
 /* Times of the last host-buffer decode (grand_engine_decode / _decode_plain):

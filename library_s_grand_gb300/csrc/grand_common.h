@@ -104,8 +104,11 @@ enum Counter {
 // packed; flagged-check counts; planning and light search; Job staging and
 // publication; result written) and search (Job / block lookup and staging; a
 // completed Job's result).
+// The ends line also keeps the latest start of a per-shot-path shot, the longest
+// per-shot-path shot and the longest tile draw (durations in ns).
 enum ProfWord { kProfChunk = 0, kProfShot = 1, kProfTiles = 2, kProfWait = 3, kProfKinds = 4,
-                kProfSteps = 4, kProfStart = 5,
+                kProfSteps = 4, kProfStart = 5, kProfLastShotStart = 6, kProfLongestShot = 7,
+                kProfLongestTiles = 8,
                 kProfChunkRead = 6, kProfChunkTest = 7, kProfChunkWrite = 8,
                 kProfShotPack = 9, kProfShotCounts = 10, kProfShotLight = 11,
                 kProfShotPublish = 12, kProfShotFinish = 13,

@@ -197,6 +197,12 @@ __global__ void __launch_bounds__(kDecodeWarps * 32, kDecodeMinBlocks) decode_ke
       atomicAdd(psum + kind, t - t_step);
       atomicAdd(psum + kProfSteps, 1ull);
       atomicMax(pend + kind, t);
+      if (step == kStepShot) {
+        atomicMax(pend + kProfLastShotStart, t_step);
+        atomicMax(pend + kProfLongestShot, t - t_step);
+      } else if (step == kStepTiles) {
+        atomicMax(pend + kProfLongestTiles, t - t_step);
+      }
       t_busy += t - t_step;
     }
   }

@@ -362,6 +362,9 @@ int grand_engine_launch_stats(GrandEngine *e, void *stream, long long *out) {
   for (int i = 0; i < kProfDetails; ++i) out[14 + i] = (long long)pa[kProfChunkRead + i];
   const unsigned long long *pm = c.data() + kCtrProfMore * kCtrStride;
   for (int i = 0; i < kProfPubWords; ++i) out[24 + i] = (long long)pm[i];
+  out[28] = pb[kProfLastShotStart] ? (long long)(pb[kProfLastShotStart] - t0) : -1;
+  out[29] = (long long)pb[kProfLongestShot];
+  out[30] = (long long)pb[kProfLongestTiles];
   return 0;
 }
 

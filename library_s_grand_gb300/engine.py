@@ -157,7 +157,7 @@ class Engine:
     def launch_stats(self, stream=0):
         """(settled by classification, per-shot path, Jobs, tiles, scratch words) of the
         last device decode on `stream`."""
-        out = (ctypes.c_longlong * 28)()
+        out = (ctypes.c_longlong * 31)()
         rc = self.lib.grand_engine_launch_stats(self.h, stream or None, out)
         return tuple(out[:5]) if rc == 0 else None
 
@@ -165,7 +165,7 @@ class Engine:
         """Phase profile of the last device decode on `stream` (the engine created
         with GRAND_PROFILE=1): warp-ns per kind of work, when the last of each kind
         ended (ns after the first warp started) and the number of work steps."""
-        out = (ctypes.c_longlong * 28)()
+        out = (ctypes.c_longlong * 31)()
         rc = self.lib.grand_engine_launch_stats(self.h, stream or None, out)
         if rc != 0:
             return None
@@ -174,7 +174,9 @@ class Engine:
                  "shot_light", "shot_publish", "shot_finish", "tile_setup", "tile_finish")
         return {"warp_ns": dict(zip(kinds, out[5:9])), "last_end_ns": dict(zip(kinds, out[9:13])),
                 "steps": out[13], "split_warp_ns": dict(zip(parts, out[14:24])),
-                "publish_warp_ns": dict(zip(("reserve", "stage", "write", "ready"), out[24:28]))}
+                "publish_warp_ns": dict(zip(("reserve", "stage", "write", "ready"), out[24:28])),
+                "last_shot_start_ns": out[28], "longest_shot_ns": out[29],
+                "longest_tile_draw_ns": out[30]}
 
     def batch_times(self):
         """(h2d, triage, search, d2h) ms of the last host-buffer decode."""
