@@ -1,7 +1,7 @@
-// grand_kernels.cuh -- what the triage and search kernels share: launch
-// constants, the per-shot result writer and the first-hit winner lookup.  The
-// two kernels live in their own translation units (grand_triage.cu,
-// grand_search.cu) so they compile in parallel.
+// grand_kernels.cuh -- what the decode kernel's work steps share (classification,
+// the per-shot path and the search, grand_decode.cuh): launch constants, the
+// per-warp shared area, bounded waits, the Job front, the per-shot result writer
+// and the first-hit winner lookup.
 #pragma once
 
 #include <cuda_runtime.h>

@@ -24,10 +24,10 @@
 //          the sketch) are key/pos[bst[b] .. bst[b+1])
 //   key    the tam sketches grouped by bucket
 //   pos    their active-list indices (u16)
-// A probe reads one filter word; only when all three of its bits are set (for a
-// prefix that matches nothing, about (3 tam / 2^F)^3: once per tens of thousands
-// of prefixes at tam ~ 100) does it walk the bucket, so the lanes of a warp
-// rarely wait for one another there.
+// A probe reads one filter word; only when all three of its bits are set does it
+// walk the bucket.  A word holds the bits of Poisson(tam / 2^(F-5)) columns, so a
+// prefix that matches nothing passes with probability about
+// E[(3b/32)^3], b ~ Poisson(tam / 2^(F-5)): one in ~7000 at tam = 126 (F = 15).
 #pragma once
 
 #include "grand_device.cuh"

@@ -7,7 +7,9 @@
 //     wakes it), copies each request's results out and wakes its waiters;
 //   * fills every free slot with the oldest waiting requests that fit
 //     (max_shots_per_batch), packs their records, and enqueues copy-in, counter
-//     reset, triage, search and copy-out on the slot's stream.
+//     reset, the decode kernel and copy-out on the slot's stream; each slot's
+//     persistent kernel gets 1/slots of the resident blocks, so all slots'
+//     kernels are on the GPU at once.
 // Requests arriving while slots run simply wait for the next free slot, so the
 // GPU always has up to `slots` micro-batches in flight.
 #include "grand_server.h"
@@ -154,7 +156,12 @@ cudaError_t start_slot(GrandServer *S, SrvSlot *sl) {
   b.light_max_log2 = e->tn.light_max_log2;
   b.tile_k = e->tn.tile_k;
   for (const DevCode &c : e->codes) b.has_ml |= c.variant == kMl;
-  if (err == cudaSuccess) err = launch_pipeline(e->ctx, b, e->tn, s);
+  // each slot's persistent grid takes its share of the resident blocks, so the
+  // slots' kernels are resident together and their batches overlap on the GPU
+  Tuning tn = e->tn;
+  const int share = std::max(1, e->ctx->decode_bps / std::max(1, (int)S->slots.size()));
+  tn.search_grid_mult = tn.search_grid_mult ? std::min(tn.search_grid_mult, share) : share;
+  if (err == cudaSuccess) err = launch_pipeline(e->ctx, b, tn, s);
   if (err == cudaSuccess)
     err = cudaMemcpyAsync(sl->h_res, sl->d_res, sizeof(GrandDecoderResult) * shot,
                           cudaMemcpyDeviceToHost, s);

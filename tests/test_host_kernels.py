@@ -1,11 +1,12 @@
-"""CPU parity of the decoding kernels themselves: grand_triage.cu and
-grand_search.cu compiled for the host (tests/host_kernels.cpp: one thread block
+"""CPU parity of the decode kernel itself: grand_decode.cuh (classification,
+per-shot path, prefix-lookup search) compiled for the host (tests/host_kernels.cpp: one thread block
 per kernel, one host thread per lane, warp collectives at a barrier) and run on
 CSS and DEM shots (uniform, prob and ML searches) whose results must equal the
 oracle's in every deterministic field, decoded pattern, logical flip and ML
-cost.  A small light budget sends most iterations through the
-search kernel (run tiles, colex tiles, the Job finisher) as well as the triage
-warp's paths (empty shots, one-position iterations, bit-mask enumeration).
+cost.  A small light budget sends most iterations through the Jobs' lookup
+search (lookup tiles, bucket walks, the Job finisher) as well as the per-shot
+paths (classification, one-position iterations, bit-mask enumeration, run
+tiles).
 Runs without a GPU."""
 import os
 import shutil
