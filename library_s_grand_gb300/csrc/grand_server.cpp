@@ -52,6 +52,7 @@ struct SrvSlot {
   // pinned host staging
   void *h_block = nullptr;
   int *h_rec = nullptr;
+  const int *in_base = nullptr;  // records read in place from here (nullptr: staged in h_rec)
   long long *h_off = nullptr;
   int *h_code = nullptr;
   GrandDecoderResult *h_res = nullptr;
@@ -109,26 +110,44 @@ void CUDART_CB slot_done(void *p) {
 // Called without the server lock; the slot is owned by the dispatcher.
 cudaError_t start_slot(GrandServer *S, SrvSlot *sl) {
   GrandEngine *e = S->eng;
+  // Where the GPU can read pageable host memory (NVLink-C2C on GB300) the kernel
+  // reads every request's records in place: offsets are taken from the lowest
+  // record address of the batch, and no record is copied on the host or to the
+  // device.  Otherwise the records are packed into the slot's pinned staging
+  // and copied in.
+  const bool in_place = e->tn.zero_copy && e->ctx->pageable_access;
+  const int *base = nullptr;
+  if (in_place)
+    for (const auto &r : sl->reqs)
+      if (!base || reinterpret_cast<uintptr_t>(r->records) < reinterpret_cast<uintptr_t>(base))
+        base = r->records;
   long long off = 0;
   int shot = 0;
   for (size_t i = 0; i < sl->reqs.size(); ++i) {
     const SrvRequest &r = *sl->reqs[i];
     sl->first[i] = shot;
+    const long long at =
+        in_place ? (long long)((reinterpret_cast<uintptr_t>(r.records) -
+                                reinterpret_cast<uintptr_t>(base)) / sizeof(int))
+                 : off;
     long long req_ints = 0;
     for (int j = 0; j < r.n; ++j) {
       const int c = r.shot_code ? r.shot_code[j] : 0;
-      sl->h_off[shot + j] = off + req_ints;
+      sl->h_off[shot + j] = at + req_ints;
       sl->h_code[shot + j] = c;
       req_ints += e->rec_len[c];
     }
-    memcpy(sl->h_rec + off, r.records, sizeof(int) * (size_t)req_ints);
+    if (!in_place) memcpy(sl->h_rec + off, r.records, sizeof(int) * (size_t)req_ints);
     off += req_ints;
     shot += r.n;
   }
   sl->nshots = shot;
+  sl->in_base = base;
   cudaStream_t s = sl->s;
-  cudaError_t err = cudaMemcpyAsync(sl->d_rec, sl->h_rec, sizeof(int) * (size_t)off,
-                                    cudaMemcpyHostToDevice, s);
+  cudaError_t err = cudaSuccess;
+  if (!in_place)
+    err = cudaMemcpyAsync(sl->d_rec, sl->h_rec, sizeof(int) * (size_t)off,
+                          cudaMemcpyHostToDevice, s);
   if (err == cudaSuccess)
     err = cudaMemcpyAsync(sl->d_off, sl->h_off, sizeof(long long) * shot, cudaMemcpyHostToDevice, s);
   if (err == cudaSuccess)
@@ -138,7 +157,7 @@ cudaError_t start_slot(GrandServer *S, SrvSlot *sl) {
   b.num_shots = shot;
   b.num_codes = (int)e->codes.size();
   b.codes = (const DevCode *)e->d_codes;
-  b.in = sl->d_rec;
+  b.in = in_place ? base : sl->d_rec;
   b.in_off = sl->d_off;
   b.shot_code = sl->d_code;
   b.results = sl->d_res;
@@ -181,9 +200,11 @@ void finish_slot(GrandServer *S, SrvSlot *sl, int rc) {
     BatchRequest req;
     req.num_shots = sl->nshots;
     req.codes = S->eng->codes;
-    req.h_in = sl->h_rec;
-    req.in_ints = (size_t)(sl->h_off[sl->nshots - 1] +
-                           S->eng->rec_len[sl->h_code[sl->nshots - 1]]);
+    req.h_in = sl->in_base ? sl->in_base : sl->h_rec;
+    long long extent = 0;
+    for (int i = 0; i < sl->nshots; ++i)
+      extent = std::max(extent, sl->h_off[i] + (long long)S->eng->rec_len[sl->h_code[i]]);
+    req.in_ints = (size_t)extent;
     req.h_off = sl->h_off;
     req.h_shot_code = sl->h_code;
     req.h_results = sl->h_res;

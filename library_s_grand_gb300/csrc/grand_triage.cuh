@@ -973,77 +973,104 @@ __device__ void classify_chunk(const DevBatch &b, int chunk, WarpArea &A, unsign
   uint32_t lg[kFastWords] = {0u, 0u, 0u, 0u};
   int ow = 0, epos = -1;
 
-  // ---- the records: int32 entries through coalesced ballots over the chunk's
-  //      back-to-back records, bit-packed words read directly -----------------
+  // ---- the records: int32 entries through coalesced ballots over runs of
+  //      back-to-back records, bit-packed words read directly ------------------
   const bool packed = cd.packed != 0;
   const bool any_int = __any_sync(kFull, valid && !packed);
   if (any_int) {
-    // entries this lane's shot occupies in b.in, and whether the chunk's
-    // records lie back to back in slot order
     const int rlen = (dem && !b.in_log) ? cd.R + cd.n_logicos : nbits;
-    const long long nb = __shfl_down_sync(kFull, rbase, 1);
-    const bool nv = __shfl_down_sync(kFull, valid ? 1 : 0, 1) != 0;
-    const bool joined = !valid || lane == 31 || !nv || nb == rbase + rlen;
-    const long long first = __shfl_sync(kFull, rbase, 0);
-    long long end = valid ? rbase + rlen : first;
+    // this lane's bits from a ballot array over the entries starting at `first`
+    // (and, for DEM logicals kept in their own array, from `lfirst` there)
+    auto extract = [&](long long first, long long lfirst, long long lbase) {
+      const int off = (int)(rbase - first);
+      if (errs) {
+        for (int q = 0; q < nwords; ++q) {
+          uint32_t w = flat_word(F.bits, off, q, nbits);
+          ow += __popc(w);
+          while (w) {
+            const int c = q * 32 + __ffs(w) - 1;
+            w &= w - 1u;
+            epos = c;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      const long long u = __shfl_xor_sync(kFull, end, o);
-      end = u > end ? u : end;
-    }
-    bool flat = __all_sync(kFull, joined && !(valid && packed)) && end - first <= 32ll * kFastBallots;
-    // DEM logicals in their own array: back to back by shot as well
+            for (int k = 0; k < kFastWords; ++k)
+              if (k < cd.nw) s[k] ^= __ldg(cd.cols + (size_t)c * cd.nwp + k);
+          }
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < kFastWords; ++k)
+          if (k < cd.nw) s[k] = flat_word(F.bits, off, k, cd.R);
+        if (dem) {
+#pragma unroll
+          for (int k = 0; k < kFastWords; ++k)
+            if (k < cd.nlw)
+              lg[k] = b.in_log ? flat_word(F.lbits, (int)(lbase - lfirst), k, cd.n_logicos)
+                               : flat_word(F.bits, off + cd.R, k, cd.n_logicos);
+        }
+      }
+    };
     const bool sep_log = dem && b.in_log && valid;
-    const bool any_sep = __any_sync(kFull, sep_log);
-    long long lbase = 0, lfirst = 0, lend = 0;
-    if (flat && any_sep) {
-      lbase = sep_log ? (long long)shot * cd.n_logicos : 0;
+    if (__any_sync(kFull, sep_log)) {
+      // DEM logicals in their own array: both arrays back to back over the chunk
+      const long long nb = __shfl_down_sync(kFull, rbase, 1);
+      const bool nv = __shfl_down_sync(kFull, valid ? 1 : 0, 1) != 0;
+      const bool joined = !valid || lane == 31 || !nv || nb == rbase + rlen;
+      const long long first = __shfl_sync(kFull, rbase, 0);
+      long long end = valid ? rbase + rlen : first;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const long long u = __shfl_xor_sync(kFull, end, o);
+        end = u > end ? u : end;
+      }
+      bool flat = __all_sync(kFull, joined && !(valid && packed)) && end - first <= 32ll * kFastBallots;
+      const long long lbase = sep_log ? (long long)shot * cd.n_logicos : 0;
       const long long lnb = __shfl_down_sync(kFull, lbase, 1);
       const bool ljoined = !valid || lane == 31 || !nv || lnb == lbase + cd.n_logicos;
-      lfirst = __shfl_sync(kFull, lbase, 0);
-      lend = valid ? lbase + cd.n_logicos : lfirst;
+      const long long lfirst = __shfl_sync(kFull, lbase, 0);
+      long long lend = valid ? lbase + cd.n_logicos : lfirst;
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
         const long long u = __shfl_xor_sync(kFull, lend, o);
         lend = u > lend ? u : lend;
       }
-      flat = __all_sync(kFull, ljoined && sep_log == (valid && dem)) &&
+      flat = flat && __all_sync(kFull, ljoined && sep_log == (valid && dem)) &&
              lend - lfirst <= 32ll * kFastLogBallots;
-    }
-    if (flat) {
-      flat_ballots(b.in + first, (int)(end - first), F.bits);
-      if (any_sep) flat_ballots(b.in_log + lfirst, (int)(lend - lfirst), F.lbits);
-      __syncwarp();
-      if (ok) {
-        const int off = (int)(rbase - first);
-        if (errs) {
-          for (int q = 0; q < nwords; ++q) {
-            uint32_t w = flat_word(F.bits, off, q, nbits);
-            ow += __popc(w);
-            while (w) {
-              const int c = q * 32 + __ffs(w) - 1;
-              w &= w - 1u;
-              epos = c;
-#pragma unroll
-              for (int k = 0; k < kFastWords; ++k)
-                if (k < cd.nw) s[k] ^= __ldg(cd.cols + (size_t)c * cd.nwp + k);
-            }
-          }
-        } else {
-#pragma unroll
-          for (int k = 0; k < kFastWords; ++k)
-            if (k < cd.nw) s[k] = flat_word(F.bits, off, k, cd.R);
-          if (dem) {
-#pragma unroll
-            for (int k = 0; k < kFastWords; ++k)
-              if (k < cd.nlw)
-                lg[k] = b.in_log ? flat_word(F.lbits, (int)(lbase - lfirst), k, cd.n_logicos)
-                                 : flat_word(F.bits, off + cd.R, k, cd.n_logicos);
-          }
-        }
+      if (flat) {
+        flat_ballots(b.in + first, (int)(end - first), F.bits);
+        flat_ballots(b.in_log + lfirst, (int)(lend - lfirst), F.lbits);
+        __syncwarp();
+        if (ok) extract(first, lfirst, lbase);
+      } else {
+        ok = ok && packed;  // records that are not back to back: slow path
       }
     } else {
-      ok = ok && packed;  // int32 records that are not back to back: slow path
+      // Runs of consecutive lanes whose int32 records lie back to back (one run
+      // for a batch packed in slot order; a few where requests' records sit in
+      // separate buffers): each run's entries through one pass of ballots.
+      const bool mine = valid && !packed;
+      const long long pend = __shfl_up_sync(kFull, rbase + rlen, 1);
+      const bool pint = __shfl_up_sync(kFull, mine ? 1 : 0, 1) != 0;
+      const unsigned members_all = __ballot_sync(kFull, mine);
+      unsigned starts = __ballot_sync(kFull, mine && (lane == 0 || !pint || pend != rbase));
+      while (starts) {
+        const int l0 = __ffs(starts) - 1;
+        starts &= starts - 1u;
+        const int lnext = starts ? __ffs(starts) - 1 : 32;
+        const unsigned span = (lnext == 32 ? kFull : ((1u << lnext) - 1u)) & ~((1u << l0) - 1u);
+        const unsigned members = members_all & span;  // l0 .. the run's last lane, no gaps
+        const int llast = 31 - __clz(members);
+        const long long first = __shfl_sync(kFull, rbase, l0);
+        const long long end = __shfl_sync(kFull, rbase + rlen, llast);
+        const bool in_run = (members >> lane) & 1u;
+        if (end - first > 32ll * kFastBallots) {
+          if (in_run) ok = false;  // longer than the chunk's ballot area: slow path
+          continue;
+        }
+        flat_ballots(b.in + first, (int)(end - first), F.bits);
+        __syncwarp();
+        if (in_run && ok) extract(first, 0, 0);
+        __syncwarp();  // every lane has read the run's bits before the next run's
+      }
     }
   }
   if (ok && packed) {
