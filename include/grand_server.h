@@ -10,7 +10,11 @@
  * and starts one on every free slot, so requests that arrive while others are on
  * the GPU join the next micro-batch and their work overlaps on the device with
  * the batches already running.  Results are identical to decoding each request
- * alone with grand_engine_decode.
+ * alone with grand_engine_decode.  Where the GPU can read pageable host memory
+ * (NVLink-C2C on GB300), the decode kernel reads each request's records where
+ * the caller keeps them, with no host or host-to-device copy of records; each
+ * slot's persistent kernel takes 1/slots of the resident blocks, so the slots'
+ * batches run on the GPU together.
  */
 #ifndef GRAND_SERVER_H
 #define GRAND_SERVER_H
