@@ -193,9 +193,14 @@ def _write_code(d, H, variant, kind, cfg, masks, Ho=None, L=None, llr_path=None)
         shutil.copy(llr_path, os.path.join(d, "llr.txt"))
 
 
-def test_mixed_codes_in_one_batch(emulator, port, tmp_path):
+@pytest.mark.parametrize("layout", ["slot_order", "code_order"])
+def test_mixed_codes_in_one_batch(emulator, port, tmp_path, layout):
     """Three codes in one shuffled batch (per-shot code and record offsets, as the
-    engine launches them): each shot's result equals the oracle's for its code."""
+    engine launches them): each shot's result equals the oracle's for its code.
+    slot_order: the records lie back to back in launch-slot order (as the engine
+    packs them); code_order: they stay in per-code order while the slots are
+    shuffled, so the records of a chunk's lanes form many separate runs (as the
+    server reads requests' buffers in place)."""
     c72, c108 = synth.BB_CODES[72](), synth.BB_CODES[108]()
     dem = synth.random_dem(4, detectors=40, mechanisms=160, logicals=5, p_range=(4e-3, 3e-2))
     e72 = synth.css_shots(c72.hz, 70, 0.03, seed=31)[0]
@@ -215,9 +220,16 @@ def test_mixed_codes_in_one_batch(emulator, port, tmp_path):
     codes = [0] * 70 + [1] * 70 + [2] * 70
     order = np.random.default_rng(34).permutation(len(records))
     flat, off = [], []
-    for i in order:
-        off.append(len(flat))
-        flat.extend(records[i])
+    if layout == "slot_order":
+        for i in order:
+            off.append(len(flat))
+            flat.extend(records[i])
+    else:
+        start = []
+        for r in records:
+            start.append(len(flat))
+            flat.extend(r)
+        off = [start[i] for i in order]
     N = len(order)
     with open(d / "mixed.txt", "w") as f:
         f.write(f"3 {N} 3 4\n")
@@ -226,6 +238,8 @@ def test_mixed_codes_in_one_batch(emulator, port, tmp_path):
     np.asarray([codes[i] for i in order], dtype=np.int32).tofile(d / "code.bin")
     out = subprocess.run([emulator, str(d)], capture_output=True, text=True, timeout=600)
     assert out.returncode == 0, out.stderr + out.stdout
+    # "ok N shots, J jobs, S slow": shots settled by the chunk step in either layout
+    assert int(out.stdout.split()[5]) < N, out.stdout
     res = np.fromfile(d / "res.bin", dtype=capi.RESULT_DTYPE)
     assert int(out.stdout.split()[3]) > 0, out.stdout  # the search kernel had Jobs
     got = np.empty(N, dtype=capi.RESULT_DTYPE)
