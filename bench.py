@@ -411,7 +411,7 @@ def run_ours(args):
 
 # DRAM bytes (read + write) of one decode_kernel launch on the headline batch, from an ncu
 # --set full capture (profiles/decode_kernel_prob_cc_bb144_16384.md).
-TRIAGE_TRAFFIC = 9.659904e6 + 768.0
+TRIAGE_TRAFFIC = 9.663744e6 + 512.0
 
 
 def hbm_peak():
@@ -441,7 +441,7 @@ STRESS_SHOTS = 192
 SKETCH_OPS_PER_CANDIDATE = 1.5
 # DRAM bytes (read + write) of one decode_kernel launch on the 192 stress shots, from an
 # ncu --set full capture (profiles/decode_kernel_stress_bb144_w4.md), per shot.
-STRESS_TRAFFIC_PER_SHOT = (289024.0 + 7936.0) / 192
+STRESS_TRAFFIC_PER_SHOT = (290048.0 + 8448.0) / 192
 # The lookup search's bound per prefix probe: two shared-memory words (the last
 # element's sketch and one filter word) at 32 words per SM per clock.
 PROBE_WORDS = 2
@@ -495,7 +495,7 @@ def stress_roofline(torch, lib, dev, sp):
     achieved = rate * SKETCH_OPS_PER_CANDIDATE
     return {"bound": "int_alu", "achieved": achieved / 1e9, "peak": peak / 1e9, "unit": "Gop/s",
             "frac": achieved / peak, "traffic": STRESS_TRAFFIC_PER_SHOT * n,
-            "traffic_unit": "bytes per launch (ncu, scaled from 48 shots)",
+            "traffic_unit": "bytes per launch (ncu capture of the same 192 shots)",
             "kernel": "decode_kernel",
             "workload": f"{n} random-syndrome shots of BB[[144,12,12]], W=4, exhaustive "
                         f"({cands} candidates, 3 threshold iterations)",
