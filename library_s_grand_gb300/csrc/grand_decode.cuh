@@ -55,7 +55,8 @@ __global__ void __launch_bounds__(kDecodeWarps * 32, kDecodeMinBlocks) decode_ke
   // changes only once every warp of the launch has left)
   const unsigned epoch = *reinterpret_cast<volatile unsigned *>(b.epoch);
   const unsigned tag = epoch + 1u;
-  const unsigned long long nchunks = b.fast ? (unsigned long long)((b.num_shots + 31) / 32) : 0ull;
+  const unsigned long long nchunks =
+      b.fast ? (unsigned long long)((b.num_shots + kChunkShots - 1) / kChunkShots) : 0ull;
   const unsigned long long nwarps = (unsigned long long)gridDim.x * kDecodeWarps;
   constexpr unsigned long long kTileMask = (1ull << 40) - 1ull;
   unsigned long long ticket = kNone;            // lane 0: a slow-queue ticket not yet used

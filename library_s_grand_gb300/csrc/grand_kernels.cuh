@@ -19,6 +19,9 @@ constexpr int kLightWords = kLightTam * 8;      // its staged column words (nwp 
 // end (the rest of the warp's area holds the syndrome and the degeneracy delta)
 constexpr int kWarpStage = 2720;
 constexpr int kTilesPerFetch = 16;  // most tiles a search warp draws at once
+// Launch slots per classification chunk (one lane each): fewer than 32 spreads a
+// batch's classification over more warps, so it ends sooner.
+constexpr int kChunkShots = 32;
 constexpr int kRunKKLight = 4;  // prefixes per lane in a run tile of the triage warp's light search
 
 // Per-warp shared memory of the decode kernel.  A warp does one kind of work at

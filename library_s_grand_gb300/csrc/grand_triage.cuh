@@ -1,7 +1,7 @@
 // grand_triage.cuh -- the per-shot work of a decoding launch (sm_103a), run by
 // the warps of the persistent decode kernel (grand_decode.cuh).
 //
-// classify_chunk (32 launch slots, one lane per shot)
+// classify_chunk (kChunkShots launch slots, one lane per shot)
 //   packs the 32 shots' records with coalesced ballots, forms each syndrome and
 //   settles the common shots outright: an empty syndrome (grand_decoder.cu:1223-1241),
 //   and a first threshold iteration with one active position whose column equals
@@ -937,7 +937,7 @@ __device__ __forceinline__ bool one_position_searched(const DevCode &cd, bool *g
   return false;
 }
 
-// Settles the shots of launch slots 32*chunk .. 32*chunk+31 that need no search
+// Settles the shots of launch slots kChunkShots*chunk + [0, kChunkShots) that need no search
 // -- an empty syndrome, or a first iteration with one active position whose
 // column equals the syndrome -- and appends the others to the slow queue.  The
 // results are exactly those of triage_shot: the one position is the only
@@ -954,8 +954,8 @@ __device__ void classify_chunk(const DevBatch &b, int chunk, WarpArea &A, unsign
   FastArea &F = *reinterpret_cast<FastArea *>(&A);
   const int lane = threadIdx.x & 31;
   const unsigned lt_mask = (1u << lane) - 1u;
-  const int slot = chunk * 32 + lane;
-  const bool valid = slot < b.num_shots;
+  const int slot = chunk * kChunkShots + lane;
+  const bool valid = lane < kChunkShots && slot < b.num_shots;
   const unsigned long long t_start = global_ns();
   unsigned long long tp = b.profile ? t_start : 0ull;
   const int shot = valid ? (b.shot_map ? b.shot_map[slot] : slot) : 0;
