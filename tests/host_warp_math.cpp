@@ -1,10 +1,13 @@
-// Host build of the search kernels' warp-level device code (csrc/grand_device.cuh)
+// Host build of the search's warp-level device code (csrc/grand_device.cuh,
+// csrc/grand_lookup.cuh)
 // on an emulated warp: 32 host threads, one per lane, whose warp collectives
 // (ballot, shuffles, reductions, votes, __syncwarp) meet at a barrier, so code
 // that keeps its lanes converged at every collective runs as on the GPU.
 // Checked against plain combinatorics and brute force: the 32-way warp search,
 // the warp-parallel lexicographic unranking of the result writer, the warp
-// minima, and whole masked colex tiles (weights 1-6) first-hit and ML.
+// minima, whole masked colex tiles (weights 1-6) first-hit and ML, the lookup
+// tables (csrc/grand_lookup.cuh) and whole lookup tiles (weights 1-6) first-hit
+// and ML.
 // Prints "ok" or the first mismatch (exit 1).
 #include <cuda_runtime.h>
 
@@ -16,6 +19,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <functional>
+#include <mutex>
 #include <random>
 #include <thread>
 #include <vector>
@@ -125,8 +129,44 @@ static inline T __ldg(const T *p) {
 }
 static inline unsigned min(unsigned a, unsigned b) { return a < b ? a : b; }
 static inline int min(int a, int b) { return a < b ? a : b; }
+template <class T>
+static inline T __shfl_up_sync(unsigned, T x, unsigned d) {
+  unsigned long long u = 0;
+  memcpy(&u, &x, sizeof(T));
+  return collective(u, [d](const unsigned long long *v, unsigned lane) {
+    T r;
+    memcpy(&r, &v[lane >= d ? lane - d : lane], sizeof(T));
+    return r;
+  });
+}
+static inline unsigned atomicOr(unsigned *a, unsigned v) {
+  return __atomic_fetch_or(a, v, __ATOMIC_SEQ_CST);
+}
+static inline unsigned atomicAdd(unsigned *a, unsigned v) {
+  return __atomic_fetch_add(a, v, __ATOMIC_SEQ_CST);
+}
+// the host build of the device headers (global timer, shared-memory loads and
+// the 128-bit CAS swapped for host equivalents)
+#define GRAND_HOST_EMULATION 1
+static inline void grand_host_cas128(unsigned long long *slot, unsigned long long c0,
+                                     unsigned long long c1, unsigned long long n0,
+                                     unsigned long long n1, unsigned long long *g0,
+                                     unsigned long long *g1) {
+  static std::mutex mu;
+  std::lock_guard<std::mutex> lk(mu);
+  *g0 = slot[0];
+  *g1 = slot[1];
+  if (slot[0] == c0 && slot[1] == c1) {
+    slot[0] = n0;
+    slot[1] = n1;
+  }
+}
+#ifndef __noinline__
+#define __noinline__ __attribute__((noinline))
+#endif
 
 #include "grand_device.cuh"
+#include "grand_lookup.cuh"
 
 using namespace grand;
 
@@ -333,5 +373,164 @@ int main() {
   }
   if (cases < 60 || matched < 15) FAIL("too few colex-tile cases: %d (%d matched)", cases, matched);
   printf("ok %d colex-tile cases\n", cases);
+
+  // lookup tables: every column is found through the filter and its bucket, the
+  // buckets partition the columns by their sketch's top bits, and a sketch that
+  // is no column passes the filter about as rarely as the layout promises
+  std::vector<uint32_t> stage(4096);
+  for (int tam : {1, 2, 5, 17, 31, 64, 126, 300, 700, 1500, 2048}) {
+    std::vector<uint32_t> hc(tam);
+    for (auto &v : hc) v = (uint32_t)rng();
+    if (tam > 3) hc[tam - 1] = hc[1];  // two columns with one sketch
+    const LookLayout L = look_layout(tam, 2720);
+    std::vector<uint32_t> blk((size_t)L.words + 4, 0xdeadbeefu);
+    for (int i = 0; i < tam; ++i) blk[i] = hc[i];
+    if (!run_warp([&](unsigned) {
+          build_lookup(blk.data(), tam, L);
+          return true;
+        }))
+      FAIL("build_lookup failed");
+    const LookView lk = look_view(blk.data(), L);
+    const int nb = 1 << L.B;
+    if (lk.bst[0] != 0u || lk.bst[nb] != (uint32_t)tam) FAIL("bucket bounds tam=%d", tam);
+    for (int b = 0; b < nb; ++b) {
+      if (lk.bst[b] > lk.bst[b + 1]) FAIL("bucket bounds not monotone tam=%d", tam);
+      for (uint32_t e = lk.bst[b]; e < lk.bst[b + 1]; ++e)
+        if ((lk.key[e] >> lk.shift) != (uint32_t)b || hc[lk.pos[e]] != lk.key[e])
+          FAIL("bucket entry tam=%d b=%d", tam, b);
+    }
+    for (int i = 0; i < tam; ++i) {
+      const uint32_t m = bloom_bits(hc[i], L.F);
+      if ((lk.filt[hc[i] & lk.wmask] & m) != m) FAIL("filter misses column %d tam=%d", i, tam);
+      const uint32_t b = hc[i] >> lk.shift;
+      bool seen = false;
+      for (uint32_t e = lk.bst[b]; e < lk.bst[b + 1]; ++e) seen = seen || (lk.pos[e] == i);
+      if (!seen) FAIL("bucket misses column %d tam=%d", i, tam);
+    }
+    int pass = 0;
+    const int probes = 200000;
+    for (int q = 0; q < probes; ++q) {
+      const uint32_t h = (uint32_t)rng();
+      const uint32_t m = bloom_bits(h, L.F);
+      pass += (lk.filt[h & lk.wmask] & m) == m;
+    }
+    // each word holds Poisson(tam / 2^(F-5)) columns' three bits: E[(3b/32)^3] bounds
+    // the pass rate of a random sketch from above (bits can coincide)
+    const double lam = (double)tam / (double)(1 << (L.F - 5));
+    const double bound = 27.0 / 32768.0 * (lam * lam * lam + 3 * lam * lam + lam);
+    if ((double)pass / probes > 2.0 * bound + 1e-4) FAIL("filter pass rate %g > %g tam=%d", (double)pass / probes, bound, tam);
+  }
+  printf("ok lookup tables\n");
+
+  // lookup tiles (the Jobs' search) against brute force, first-hit and ML
+  int lcases = 0, lmatched = 0;
+  for (int trial = 0; trial < 90; ++trial) {
+    const int tam = 1 + (int)(rng() % 140);
+    const int w = 1 + (int)(rng() % 6);
+    if (w > tam || C(tam, w) > 3000000ull) continue;
+    const int R = 6 + (int)(rng() % 90), nw = (R + 31) / 32, nwp = nw == 1 ? 1 : (nw == 2 ? 2 : 4);
+    std::vector<uint32_t> cols((size_t)tam * nwp, 0u), hc(tam), sw(32, 0u);
+    for (int c = 0; c < tam; ++c)
+      for (int r = 0; r < R; ++r)
+        if (rng() % 4 == 0) cols[(size_t)c * nwp + r / 32] |= 1u << (r % 32);
+    if (rng() % 3 == 0) {
+      const int a = (int)(rng() % tam), b = (int)(rng() % tam);
+      for (int i = 0; i < nwp; ++i) cols[(size_t)a * nwp + i] = cols[(size_t)b * nwp + i];
+    }
+    if (rng() % 4) {
+      std::vector<int> pick(tam);
+      for (int i = 0; i < tam; ++i) pick[i] = i;
+      std::shuffle(pick.begin(), pick.end(), rng);
+      for (int e = 0; e < w; ++e)
+        for (int i = 0; i < nw; ++i) sw[i] ^= cols[(size_t)pick[e] * nwp + i];
+    } else {
+      for (int i = 0; i < nw; ++i) sw[i] = (uint32_t)rng();
+      if (R % 32) sw[nw - 1] &= (1u << (R % 32)) - 1u;
+    }
+    auto sketch = [&](const uint32_t *v) {
+      uint32_t h = 0;
+      for (int r = 0; r < R; ++r)
+        if ((v[r / 32] >> (r % 32)) & 1u) h ^= row_hash(r);
+      return h;
+    };
+    for (int c = 0; c < tam; ++c) hc[c] = sketch(&cols[(size_t)c * nwp]);
+    std::vector<float> llr(tam);
+    for (auto &v : llr) v = (float)(1 + rng() % 6) * 0.25f;
+    const LookLayout L = look_layout(tam, 2720);
+    std::vector<uint32_t> blk((size_t)L.words + 8, 0u);
+    for (int i = 0; i < tam; ++i) blk[i] = hc[i];
+    if (!run_warp([&](unsigned) {
+          build_lookup(blk.data(), tam, L);
+          return true;
+        }))
+      FAIL("build_lookup failed");
+    const LookView lk = look_view(blk.data(), L);
+    const SegView sv{blk.data(), cols.data(), llr.data(), sketch(sw.data()), tam, w, kLookK,
+                     nwp, nw, C(tam - 1, w - 1), 700ull};
+    const unsigned long long ntiles = lookup_tiles(sv.nprefix);
+    unsigned long long bg = kNone, br = kNone;
+    uint32_t bo = 0xffffffffu;
+    {
+      std::vector<int> x(w);
+      for (int i = 0; i < w; ++i) x[i] = i;
+      for (unsigned long long r = 0;; ++r) {
+        bool eq = true;
+        for (int i = 0; i < nw && eq; ++i) {
+          uint32_t z = sw[i];
+          for (int e = 0; e < w; ++e) z ^= cols[(size_t)x[e] * nwp + i];
+          eq = z == 0u;
+        }
+        if (eq) {
+          if (bg == kNone) bg = sv.base + r;
+          float cst = 0.0f;
+          for (int e = 0; e < w; ++e) cst = cst + llr[x[e]];
+          const uint32_t k2 = cost_key(cst);
+          if (k2 < bo || (k2 == bo && r < br)) {
+            bo = k2;
+            br = r;
+          }
+        }
+        int i = w - 1;
+        while (i >= 0 && x[i] == tam - w + i) --i;
+        if (i < 0) break;
+        ++x[i];
+        for (int j = i + 1; j < w; ++j) x[j] = x[j - 1] + 1;
+      }
+    }
+    for (int ml = 0; ml < 2; ++ml) {
+      unsigned long long got_g = kNone, got_r = kNone;
+      uint32_t got_o = 0xffffffffu;
+      const bool ok = run_warp([&](unsigned) {
+        LaneBest acc;
+        acc.reset();
+        for (unsigned long long tile = 0; tile < ntiles; ++tile) {
+          const LaneBest lb = ml ? eval_lookup_tile<kLookK, true, true>(sv, lk, t.data(), sw.data(), tile)
+                                 : eval_lookup_tile<kLookK, false, true>(sv, lk, t.data(), sw.data(), tile);
+          if (lb.g < acc.g) acc.g = lb.g;
+          if (lb.o < acc.o || (lb.o == acc.o && lb.r < acc.r)) {
+            acc.o = lb.o;
+            acc.r = lb.r;
+          }
+        }
+        const unsigned long long g = warp_min_u64(acc.g);
+        uint32_t o = acc.o;
+        unsigned long long r = acc.r;
+        warp_min_key(o, r);
+        if ((threadIdx.x & 31) == 0) {
+          got_g = g;
+          got_o = o;
+          got_r = r;
+        }
+        return true;
+      });
+      if (!ok) FAIL("lookup tile run failed");
+      if (!ml && got_g != bg) FAIL("lookup tiles first-hit tam=%d w=%d: %llu vs %llu", tam, w, got_g, bg);
+      if (ml && (got_o != bo || got_r != br)) FAIL("lookup tiles ML tam=%d w=%d", tam, w);
+    }
+    ++lcases;
+    lmatched += bg != kNone;
+  }
+  if (lcases < 50 || lmatched < 25) FAIL("too few lookup-tile cases: %d (%d matched)", lcases, lmatched);
+  printf("ok %d lookup-tile cases\n", lcases);
   return 0;
 }

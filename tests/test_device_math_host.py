@@ -1,12 +1,15 @@
-"""The search kernels' device code, compiled for the host from the CUDA header
-itself (csrc/grand_device.cuh) and checked against plain combinatorics and a
+"""The search's device code, compiled for the host from the CUDA headers
+themselves (csrc/grand_device.cuh, csrc/grand_lookup.cuh) and checked against plain combinatorics and a
 brute-force search, without a GPU:
   tests/host_device_math.cpp  warp-free math: binomials, colex unranking in
       closed form and by table, colex successors, lexicographic ranks, the FP32
       cost key, and whole run tiles lane by lane, first-hit and ML;
   tests/host_warp_math.cpp    warp-level code on an emulated warp (32 host
       threads whose collectives meet at a barrier): the warp minima, the result
-      writer's warp-parallel unranking, and whole masked colex tiles."""
+      writer's warp-parallel unranking, whole masked colex tiles, the lookup
+      tables (csrc/grand_lookup.cuh: filter and buckets hold every column, the
+      filter's false-pass rate stays under its bound) and whole lookup tiles of
+      weights 1-6 against brute force, first-hit and ML."""
 import os
 import shutil
 import subprocess
