@@ -6,7 +6,10 @@
  * in-flight slots, each with its own CUDA stream and device workspace sized at
  * creation (admission by memory: the slots must fit the HBM budget and the free
  * device memory).  A dispatcher thread keeps forming micro-batches from the
- * requests waiting in arrival order -- shots of different codes mix freely --
+ * requests waiting in arrival order -- shots of different codes mix freely, and
+ * a request is admitted into a micro-batch while the batch's shots fit the slot
+ * and the search scratch they are expected to stage (the scratch per shot of
+ * the server's recent batches) fits 3/4 of the slot's arena --
  * and starts one on every free slot, so requests that arrive while others are on
  * the GPU join the next micro-batch and their work overlaps on the device with
  * the batches already running.  Results are identical to decoding each request

@@ -6,7 +6,10 @@
 //   * reaps slots whose work finished (a host callback on the slot's stream
 //     wakes it), copies each request's results out and wakes its waiters;
 //   * fills every free slot with the oldest waiting requests that fit
-//     (max_shots_per_batch), packs their records, and enqueues copy-in, counter
+//     (max_shots_per_batch, and the search scratch expected from the recent
+//     batches' scratch per shot within 3/4 of the slot's arena), packs their
+//     offsets (records are read in place where the GPU can reach pageable
+//     memory, copied through pinned staging otherwise), and enqueues copy-in, counter
 //     reset, the decode kernel and copy-out on the slot's stream; each slot's
 //     persistent kernel gets 1/slots of the resident blocks, so all slots'
 //     kernels are on the GPU at once.
@@ -57,6 +60,7 @@ struct SrvSlot {
   int *h_code = nullptr;
   GrandDecoderResult *h_res = nullptr;
   unsigned *h_status = nullptr;
+  unsigned long long *h_top = nullptr;  // scratch words the last batch staged
   // device buffers
   void *d_block = nullptr;
   int *d_rec = nullptr;
@@ -92,6 +96,10 @@ struct GrandServer {
   std::deque<std::shared_ptr<SrvRequest>> queue;
   std::unordered_map<unsigned long long, std::shared_ptr<SrvRequest>> live;
   unsigned long long next_id = 1;
+  // Search scratch staged per shot on recent batches (moving average): the
+  // dispatcher admits requests into a micro-batch while the expected scratch
+  // stays within the arena's headroom.
+  double scratch_per_shot = 0.0;
   bool stop = false;
   std::thread th;
 };
@@ -186,6 +194,9 @@ cudaError_t start_slot(GrandServer *S, SrvSlot *sl) {
                           cudaMemcpyDeviceToHost, s);
   if (err == cudaSuccess)
     err = cudaMemcpyAsync(sl->h_status, b.status, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+  if (err == cudaSuccess)
+    err = cudaMemcpyAsync(sl->h_top, ctr_ptr(b.counters, kCtrScratchTop), sizeof(unsigned long long),
+                          cudaMemcpyDeviceToHost, s);
   sl->completed.store(0);
   if (err == cudaSuccess) err = cudaLaunchHostFunc(s, slot_done, sl);
   return err;
@@ -212,6 +223,14 @@ void finish_slot(GrandServer *S, SrvSlot *sl, int rc) {
     if (ws) S->eng->ctx->release(ws);
   } else if (rc == 0 && (*sl->h_status & kStatusTamLimit)) {
     rc = GRAND_ERR_LIMIT;
+  }
+  if (rc == 0 && sl->nshots > 0) {
+    // an overflowing batch staged at least the whole arena
+    const double top = (*sl->h_status & kStatusScratchOverflow) ? (double)kSrvArenaWords
+                                                                 : (double)*sl->h_top;
+    const double per = top / (double)sl->nshots;
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->scratch_per_shot = S->scratch_per_shot == 0.0 ? per : 0.75 * S->scratch_per_shot + 0.25 * per;
   }
   const Clock::time_point now = Clock::now();
   for (size_t i = 0; i < sl->reqs.size(); ++i) {
@@ -243,7 +262,11 @@ void dispatcher(GrandServer *S) {
       if (sl->busy || S->queue.empty()) continue;
       int shots = 0;
       sl->reqs.clear();
-      while (!S->queue.empty() && shots + S->queue.front()->n <= S->max_shots) {
+      // admission: the slot's shots, and the search scratch they are expected
+      // to stage within 3/4 of its arena (at least one request per batch)
+      const double room = 0.75 * (double)kSrvArenaWords;
+      while (!S->queue.empty() && shots + S->queue.front()->n <= S->max_shots &&
+             (shots == 0 || (shots + S->queue.front()->n) * S->scratch_per_shot <= room)) {
         shots += S->queue.front()->n;
         sl->reqs.push_back(S->queue.front());
         S->queue.pop_front();
@@ -339,6 +362,7 @@ int grand_server_create(GrandEngine *e, int slots, int max_shots, size_t budget,
     sl->h_code = (int *)(h + rec + offb);
     sl->h_res = (GrandDecoderResult *)(h + rec + offb + codeb);
     sl->h_status = (unsigned *)(h + rec + offb + codeb + resb);
+    sl->h_top = (unsigned long long *)(h + rec + offb + codeb + resb + 8);
     char *d = (char *)sl->d_block;
     sl->d_rec = (int *)d;
     d += rec;
