@@ -119,6 +119,10 @@ enum ProfWord { kProfChunk = 0, kProfShot = 1, kProfTiles = 2, kProfWait = 3, kP
 enum ProfPubWord { kProfPubReserve = 0, kProfPubStage = 1, kProfPubWrite = 2, kProfPubReady = 3,
                    kProfPubWords = 4 };
 
+// Words per shot of DevBatch::rec_cache: a record's bits as the chunk step read
+// them (error words, or syndrome / detector words then DEM logical words).
+constexpr int kRecCacheWords = 16;
+
 // Address of control word k.
 GRAND_HD inline unsigned long long *ctr_ptr(unsigned long long *counters, int k) {
   return counters + k * kCtrStride;
@@ -239,6 +243,8 @@ struct DevBatch {
   unsigned long long scratch_words;
   unsigned *status;
   int *deferred;                 // per shot: 1 if the shot must be re-run
+  uint32_t *rec_cache;           // num_shots x kRecCacheWords: a slow-queue shot's record as
+                                 // packed words, written by the chunk step (nullptr: none)
   unsigned long long *queue;     // num_shots entries: ((epoch + 1) << 32) | launch slot of a
                                  // shot that needs the per-shot path
   unsigned *epoch;               // the workspace's launch epoch (kCtlAllocBytes layout)

@@ -101,7 +101,8 @@ __global__ void __launch_bounds__(kDecodeWarps * 32, kDecodeMinBlocks) decode_ke
             }
             if ((unsigned)(v >> 32) == tag) {
               step = kStepShot;
-              a0 = v & 0xffffffffull;
+              a0 = v & 0x7fffffffull;
+              a1 = (v >> 31) & 1ull;  // the chunk step left the record's bits in rec_cache
             } else {
               atomicOr(b.status, kStatusWaitLimit);
             }
@@ -181,7 +182,8 @@ __global__ void __launch_bounds__(kDecodeWarps * 32, kDecodeMinBlocks) decode_ke
         atomicAdd(ctr_ptr(b.counters, kCtrChunksDone), 1ull);
       }
     } else if (step == kStepShot) {
-      triage_shot<MLK>(b, (int)a0, A, plans[wib], tag);
+      a1 = __shfl_sync(kFull, a1, 0);
+      triage_shot<MLK>(b, (int)a0, A, plans[wib], tag, a1 != 0ull);
       cache.stage_lost();
       if (lane == 0) {
         __threadfence();

@@ -265,6 +265,7 @@ int grand_engine_decode_device(GrandEngine *e, int num_shots, const int *d_shot_
   b.scratch_words = scratch_words;
   b.deferred = (int *)slot->d_deferred;
   b.queue = shot_queue(slot->d_deferred, num_shots);
+  b.rec_cache = shot_rec_cache(slot->d_deferred, num_shots);
   b.epoch = (unsigned *)((char *)slot->d_small + kCtlBytes);
   b.fast = e->tn.fast;
   b.profile = e->tn.profile;

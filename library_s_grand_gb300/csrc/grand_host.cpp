@@ -490,6 +490,7 @@ int run_batch(Context *ctx, Workspace *ws, const BatchRequest &req, BatchTiming 
   b.scratch_words = scratch_words;
   b.deferred = (int *)ws->d_deferred;
   b.queue = shot_queue(ws->d_deferred, N);
+  b.rec_cache = shot_rec_cache(ws->d_deferred, N);
   b.epoch = (unsigned *)((char *)ws->d_small + kCtlBytes);
   b.fast = tn.fast;
   b.profile = tn.profile;

@@ -90,13 +90,21 @@ cudaError_t ensure(void **p, size_t *cap, size_t bytes);
 cudaError_t ensure_zeroed(void **p, size_t *cap, size_t bytes);
 
 // Bytes of the per-shot buffer: num_shots re-run flags (int), then, 8-byte
-// aligned, num_shots slow-queue entries (u64).
+// aligned, num_shots slow-queue entries (u64), then, 16-byte aligned, num_shots
+// record-cache rows (kRecCacheWords words each).
+inline size_t shot_queue_offset(size_t num_shots) { return (4 * num_shots + 7) & ~(size_t)7; }
+inline size_t shot_cache_offset(size_t num_shots) {
+  return (shot_queue_offset(num_shots) + 8 * num_shots + 15) & ~(size_t)15;
+}
 inline size_t shot_buffer_bytes(size_t num_shots) {
-  return ((4 * num_shots + 7) & ~(size_t)7) + 8 * num_shots;
+  return shot_cache_offset(num_shots) + sizeof(uint32_t) * kRecCacheWords * num_shots;
 }
 inline unsigned long long *shot_queue(void *shot_buffer, size_t num_shots) {
   return reinterpret_cast<unsigned long long *>(static_cast<char *>(shot_buffer) +
-                                                ((4 * num_shots + 7) & ~(size_t)7));
+                                                shot_queue_offset(num_shots));
+}
+inline uint32_t *shot_rec_cache(void *shot_buffer, size_t num_shots) {
+  return reinterpret_cast<uint32_t *>(static_cast<char *>(shot_buffer) + shot_cache_offset(num_shots));
 }
 
 class Context {

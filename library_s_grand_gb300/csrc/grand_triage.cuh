@@ -491,7 +491,8 @@ __device__ void light_search(const DevBatch &b, const DevCode &cd, Job &J, WarpA
 // The full per-shot path: one warp, launch slot `slot`.  P is the warp's planner
 // state; tag (the launch epoch + 1) marks a published Job.
 template <bool MLK>
-__device__ void triage_shot(const DevBatch &b, int slot, WarpArea &A, PlanState &P, unsigned tag) {
+__device__ void triage_shot(const DevBatch &b, int slot, WarpArea &A, PlanState &P, unsigned tag,
+                            bool cached) {
   const int lane = threadIdx.x & 31;
   {
     const unsigned long long t_start = global_ns();
@@ -499,13 +500,16 @@ __device__ void triage_shot(const DevBatch &b, int slot, WarpArea &A, PlanState 
     const int shot = b.shot_map ? b.shot_map[slot] : slot;
     const int ci = b.shot_code ? b.shot_code[shot] : 0;
     const DevCode &cd = b.codes[ci];
-    const int *rec = b.in + (b.in_off ? b.in_off[shot] : (long long)shot * cd.rec_len);
+    // a record the chunk step already read is taken from its packed copy in
+    // rec_cache (device memory, in place of a second read of the caller's record)
+    const int *rec = cached ? reinterpret_cast<const int *>(b.rec_cache + (size_t)slot * kRecCacheWords)
+                            : b.in + (b.in_off ? b.in_off[shot] : (long long)shot * cd.rec_len);
     Job &J = A.job;
 
     // ---- pack the record ---------------------------------------------------
     uint32_t s_lane = 0;  // lane w holds syndrome word w
     int original_weight = 0;
-    if (cd.packed) {
+    if (cd.packed || cached) {
       // bit-packed records: the words are the bits (bits past the last entry ignored)
       const int nwords = cd.input_kind == kInErrors ? cd.mw : cd.nw;
       const int nbits = cd.input_kind == kInErrors ? cd.m : cd.R;
@@ -517,8 +521,9 @@ __device__ void triage_shot(const DevBatch &b, int slot, WarpArea &A, PlanState 
         original_weight += __popc(v);
       }
       if (cd.family == kDem) {
-        const uint32_t *lg = b.in_log ? reinterpret_cast<const uint32_t *>(b.in_log) + (size_t)shot * cd.nlw
-                                      : reinterpret_cast<const uint32_t *>(rec) + cd.nw;
+        const uint32_t *lg = (b.in_log && !cached)
+                                 ? reinterpret_cast<const uint32_t *>(b.in_log) + (size_t)shot * cd.nlw
+                                 : reinterpret_cast<const uint32_t *>(rec) + cd.nw;
         for (int q = lane; q < cd.nlw; q += 32) {
           uint32_t v = __ldcg(lg + q);
           if (q == cd.nlw - 1 && (cd.n_logicos & 31)) v &= (1u << (cd.n_logicos & 31)) - 1u;
@@ -883,17 +888,58 @@ struct FastArea {
 };
 static_assert(sizeof(FastArea) <= sizeof(WarpArea), "FastArea must fit the warp's area");
 
-// bits[k] = ballot(p[32k + lane] != 0) for the n entries at p (bits past n are 0),
-// sixteen words' loads issued before their ballots; bits[ceil(n/32)] = 0.
+// Bits b0..b7 of x moved to bits 0, 4, .., 28.
+__device__ __forceinline__ uint32_t spread4(uint32_t x) {
+  x &= 0xffu;
+  x = (x | (x << 12)) & 0x000F000Fu;
+  x = (x | (x << 6)) & 0x03030303u;
+  x = (x | (x << 3)) & 0x11111111u;
+  return x;
+}
+
+// bits[k] = the nonzero flags of p[32k .. 32k + 31] for the n entries at p (bits
+// past n are 0); bits[ceil(n/32)] = 0.  The entries are read once and kept out
+// of L1 (the per-shot path may read them again from L2).  With p 16-byte
+// aligned, lanes read four entries at a time, eight 16-byte loads each in
+// flight (records read in place from host memory need the bytes in flight): a
+// row of 32 lanes is 128 entries, and its four words are four ballots (ballot
+// c holds entry 4l + c in bit l) interleaved by four lanes.  Otherwise, and for
+// the last n % 128 entries, one entry per lane per ballot.
 __device__ __forceinline__ void flat_ballots(const int *p, int n, uint32_t *bits) {
   const int lane = threadIdx.x & 31;
   const int nwords = (n + 31) >> 5;
-  for (int k0 = 0; k0 < nwords; k0 += 16) {
+  int done = 0;  // entries handled by the 16-byte path (a multiple of 128)
+  if ((reinterpret_cast<uintptr_t>(p) & 15u) == 0u) {
+    const int4 *p4 = reinterpret_cast<const int4 *>(p);
+    const int rows = n >> 7;  // full rows of 128 entries
+    for (int r0 = 0; r0 < rows; r0 += 8) {
+      int4 v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+        v[u] = r0 + u < rows ? __ldcg(p4 + (r0 + u) * 32 + lane) : make_int4(0, 0, 0, 0);
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        if (r0 + u < rows) {
+          const uint32_t b0 = __ballot_sync(kFull, v[u].x != 0);
+          const uint32_t b1 = __ballot_sync(kFull, v[u].y != 0);
+          const uint32_t b2 = __ballot_sync(kFull, v[u].z != 0);
+          const uint32_t b3 = __ballot_sync(kFull, v[u].w != 0);
+          if (lane < 4) {
+            const int sh = 8 * lane;
+            bits[(r0 + u) * 4 + lane] = spread4(b0 >> sh) | (spread4(b1 >> sh) << 1) |
+                                        (spread4(b2 >> sh) << 2) | (spread4(b3 >> sh) << 3);
+          }
+        }
+      }
+    }
+    done = rows << 7;
+  }
+  for (int k0 = done >> 5; k0 < nwords; k0 += 16) {
     int v[16];
 #pragma unroll
     for (int u = 0; u < 16; ++u) {
       const int e = (k0 + u) * 32 + lane;
-      v[u] = e < n ? __ldcg(p + e) : 0;  // kept in L2: the slow path may read it again
+      v[u] = e < n ? __ldcg(p + e) : 0;
     }
     uint32_t mine = 0u;
 #pragma unroll
@@ -976,16 +1022,20 @@ __device__ void classify_chunk(const DevBatch &b, int chunk, WarpArea &A, unsign
   // ---- the records: int32 entries through coalesced ballots over runs of
   //      back-to-back records, bit-packed words read directly ------------------
   const bool packed = cd.packed != 0;
+  bool extracted = false;  // this lane's record bits are in rec_cache
   const bool any_int = __any_sync(kFull, valid && !packed);
   if (any_int) {
     const int rlen = (dem && !b.in_log) ? cd.R + cd.n_logicos : nbits;
     // this lane's bits from a ballot array over the entries starting at `first`
     // (and, for DEM logicals kept in their own array, from `lfirst` there)
+    // (and its words into rec_cache, for the per-shot path if the shot goes there)
+    uint32_t *cache = b.rec_cache ? b.rec_cache + (size_t)slot * kRecCacheWords : nullptr;
     auto extract = [&](long long first, long long lfirst, long long lbase) {
       const int off = (int)(rbase - first);
       if (errs) {
         for (int q = 0; q < nwords; ++q) {
           uint32_t w = flat_word(F.bits, off, q, nbits);
+          if (cache) cache[q] = w;
           ow += __popc(w);
           while (w) {
             const int c = q * 32 + __ffs(w) - 1;
@@ -999,15 +1049,21 @@ __device__ void classify_chunk(const DevBatch &b, int chunk, WarpArea &A, unsign
       } else {
 #pragma unroll
         for (int k = 0; k < kFastWords; ++k)
-          if (k < cd.nw) s[k] = flat_word(F.bits, off, k, cd.R);
+          if (k < cd.nw) {
+            s[k] = flat_word(F.bits, off, k, cd.R);
+            if (cache) cache[k] = s[k];
+          }
         if (dem) {
 #pragma unroll
           for (int k = 0; k < kFastWords; ++k)
-            if (k < cd.nlw)
+            if (k < cd.nlw) {
               lg[k] = b.in_log ? flat_word(F.lbits, (int)(lbase - lfirst), k, cd.n_logicos)
                                : flat_word(F.bits, off + cd.R, k, cd.n_logicos);
+              if (cache) cache[cd.nw + k] = lg[k];
+            }
         }
       }
+      extracted = cache != nullptr;
     };
     const bool sep_log = dem && b.in_log && valid;
     if (__any_sync(kFull, sep_log)) {
@@ -1228,7 +1284,7 @@ __device__ void classify_chunk(const DevBatch &b, int chunk, WarpArea &A, unsign
     // is not a leftover of an earlier launch
     if (slow)
       *reinterpret_cast<volatile unsigned long long *>(b.queue + base + __popc(sm & lt_mask)) =
-          ((unsigned long long)tag << 32) | (unsigned)slot;
+          ((unsigned long long)tag << 32) | (unsigned)slot | (extracted && ok ? 0x80000000u : 0u);
   }
   __syncwarp();
   prof_lap(b, kProfChunkWrite, tp);

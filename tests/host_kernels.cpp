@@ -425,8 +425,10 @@ static unsigned run_batch(DevBatch &b, int N) {
   scratch.assign(scratch_words, 0u);
   static std::vector<int> deferred;
   static std::vector<unsigned long long> queue;
+  static std::vector<uint32_t> rec_cache;
   deferred.assign(N, 0);
   queue.assign(std::max(N, 1), 0ull);
+  rec_cache.assign((size_t)std::max(N, 1) * kRecCacheWords, 0xa5a5a5a5u);
   b.num_shots = N;
   b.ncr = ncr.data();
   b.jobs = jobs.data();
@@ -437,6 +439,9 @@ static unsigned run_batch(DevBatch &b, int N) {
   b.scratch_words = scratch_words;
   b.deferred = deferred.data();
   b.queue = queue.data();
+  // GRAND_EMU_CACHE=0: the per-shot path reads every record again instead
+  const char *fc = getenv("GRAND_EMU_CACHE");
+  b.rec_cache = (fc && *fc == '0') ? nullptr : rec_cache.data();
   b.epoch = reinterpret_cast<unsigned *>(reinterpret_cast<char *>(small) + kCtlBytes);
   const char *fe = getenv("GRAND_EMU_FAST");
   b.fast = (fe && *fe == '0') ? 0 : 1;
