@@ -244,7 +244,8 @@ struct DevBatch {
   unsigned *status;
   int *deferred;                 // per shot: 1 if the shot must be re-run
   uint32_t *rec_cache;           // num_shots x kRecCacheWords: a slow-queue shot's record as
-                                 // packed words, written by the chunk step (nullptr: none)
+                                 // packed words, written by the chunk step (nullptr: none; set
+                                 // when records are read in place from host memory)
   unsigned long long *queue;     // num_shots entries: ((epoch + 1) << 32) | launch slot of a
                                  // shot that needs the per-shot path
   unsigned *epoch;               // the workspace's launch epoch (kCtlAllocBytes layout)

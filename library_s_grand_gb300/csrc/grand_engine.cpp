@@ -265,7 +265,9 @@ int grand_engine_decode_device(GrandEngine *e, int num_shots, const int *d_shot_
   b.scratch_words = scratch_words;
   b.deferred = (int *)slot->d_deferred;
   b.queue = shot_queue(slot->d_deferred, num_shots);
-  b.rec_cache = shot_rec_cache(slot->d_deferred, num_shots);
+  // records in device memory: the per-shot path reads them again from L2 (the
+  // record cache pays off only for records read in place from host memory)
+  b.rec_cache = nullptr;
   b.epoch = (unsigned *)((char *)slot->d_small + kCtlBytes);
   b.fast = e->tn.fast;
   b.profile = e->tn.profile;

@@ -490,7 +490,9 @@ int run_batch(Context *ctx, Workspace *ws, const BatchRequest &req, BatchTiming 
   b.scratch_words = scratch_words;
   b.deferred = (int *)ws->d_deferred;
   b.queue = shot_queue(ws->d_deferred, N);
-  b.rec_cache = shot_rec_cache(ws->d_deferred, N);
+  // records read in place from host memory: the per-shot path takes the bits the
+  // chunk step kept instead of a second read over NVLink-C2C
+  b.rec_cache = zc ? shot_rec_cache(ws->d_deferred, N) : nullptr;
   b.epoch = (unsigned *)((char *)ws->d_small + kCtlBytes);
   b.fast = tn.fast;
   b.profile = tn.profile;

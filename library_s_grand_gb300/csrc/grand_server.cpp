@@ -178,7 +178,7 @@ cudaError_t start_slot(GrandServer *S, SrvSlot *sl) {
   b.scratch_words = kSrvArenaWords;
   b.deferred = sl->d_deferred;
   b.queue = shot_queue(sl->d_deferred, S->max_shots);
-  b.rec_cache = shot_rec_cache(sl->d_deferred, S->max_shots);
+  b.rec_cache = in_place ? shot_rec_cache(sl->d_deferred, S->max_shots) : nullptr;
   b.epoch = (unsigned *)((char *)sl->d_small + kCtlBytes);
   b.fast = e->tn.fast;
   b.light_max_log2 = e->tn.light_max_log2;
