@@ -411,7 +411,7 @@ def run_ours(args):
 
 # DRAM bytes (read + write) of one decode_kernel launch on the headline batch, from an ncu
 # --set full capture (profiles/decode_kernel_prob_cc_bb144_16384.md).
-TRIAGE_TRAFFIC = 9.663744e6 + 512.0
+TRIAGE_TRAFFIC = 9.694976e6 + 768.0
 
 
 def hbm_peak():
