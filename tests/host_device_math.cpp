@@ -60,6 +60,7 @@ static inline unsigned min(unsigned a, unsigned b) { return a < b ? a : b; }
 static inline int min(int a, int b) { return a < b ? a : b; }
 
 #include "grand_device.cuh"
+#include "grand_solo.h"
 
 using namespace grand;
 
@@ -257,5 +258,58 @@ int main() {
   }
   CHECK(cases >= 200 && matched >= 50, "too few run-tile cases: %d (%d matched)", cases, matched);
   printf("ok %d run-tile cases\n", cases);
+
+  // solo-column table: exactly the nonzero columns that contain no other nonzero
+  // column (duplicates and zero columns excluded), each found by its sketch
+  int solo_codes = 0, solo_seen = 0;
+  for (int trial = 0; trial < 60; ++trial) {
+    const int R = 3 + (int)(rng() % 120), m = 1 + (int)(rng() % 200);
+    const int nw = (R + 31) / 32, nwp = nw <= 2 ? nw : (nw <= 4 ? 4 : 8);
+    std::vector<uint32_t> cols((size_t)m * nwp, 0u), hcol(m, 0u);
+    const int dens = 2 + (int)(rng() % 12);
+    for (int c = 0; c < m; ++c) {
+      if (rng() % 25 == 0) continue;  // a zero column
+      for (int r = 0; r < R; ++r)
+        if (rng() % dens == 0) cols[(size_t)c * nwp + r / 32] |= 1u << (r % 32);
+    }
+    for (int k = 0; k < 3 && m > 2; ++k) {  // duplicates and a column inside another
+      const int a = (int)(rng() % m), b = (int)(rng() % m);
+      if (k < 2) {
+        for (int i = 0; i < nwp; ++i) cols[(size_t)a * nwp + i] = cols[(size_t)b * nwp + i];
+      } else {
+        for (int i = 0; i < nwp; ++i)
+          cols[(size_t)a * nwp + i] = cols[(size_t)b * nwp + i] & (uint32_t)rng();
+      }
+    }
+    for (int c = 0; c < m; ++c)
+      for (int r = 0; r < R; ++r)
+        if ((cols[(size_t)c * nwp + r / 32] >> (r % 32)) & 1u) hcol[c] ^= row_hash(r);
+    const SoloTable t = build_solo_table(cols, nwp, nw, m, hcol);
+    auto nonzero = [&](int c) {
+      for (int i = 0; i < nw; ++i)
+        if (cols[(size_t)c * nwp + i]) return true;
+      return false;
+    };
+    auto inside = [&](int a, int b) {  // a's rows within b's
+      for (int i = 0; i < nw; ++i)
+        if (cols[(size_t)a * nwp + i] & ~cols[(size_t)b * nwp + i]) return false;
+      return true;
+    };
+    for (int c = 0; c < m; ++c) {
+      bool solo = nonzero(c);
+      for (int o = 0; o < m && solo; ++o)
+        if (o != c && nonzero(o) && inside(o, c)) solo = false;
+      bool found = false;
+      uint32_t i = hcol[c] & t.mask;
+      for (uint32_t probe = 0; probe <= t.mask && t.cols[i] >= 0; ++probe, i = (i + 1) & t.mask)
+        found = found || (t.cols[i] == c && t.keys[i] == hcol[c]);
+      CHECK(found == solo, "solo table R=%d m=%d column %d: table %d, brute force %d", R, m, c,
+            (int)found, (int)solo);
+      solo_seen += solo;
+    }
+    ++solo_codes;
+  }
+  CHECK(solo_seen > 500, "too few solo columns: %d", solo_seen);
+  printf("ok solo tables of %d codes (%d solo columns)\n", solo_codes, solo_seen);
   return 0;
 }

@@ -3,7 +3,9 @@ themselves (csrc/grand_device.cuh, csrc/grand_lookup.cuh) and checked against pl
 brute-force search, without a GPU:
   tests/host_device_math.cpp  warp-free math: binomials, colex unranking in
       closed form and by table, colex successors, lexicographic ranks, the FP32
-      cost key, and whole run tiles lane by lane, first-hit and ML;
+      cost key, whole run tiles lane by lane, first-hit and ML, and the
+      solo-column table of the classification step (csrc/grand_solo.h) against
+      its brute-force definition;
   tests/host_warp_math.cpp    warp-level code on an emulated warp (32 host
       threads whose collectives meet at a barrier): the warp minima, the result
       writer's warp-parallel unranking, whole masked colex tiles, the lookup
