@@ -152,7 +152,7 @@ struct BatchTiming {
 
 // Tunables (environment overrides, autotuner results).
 struct Tuning {
-  int light_max_log2 = 12;
+  int light_max_log2 = 10;
   int tile_k = 4;
   int search_grid_mult = 0;  // CTAs per SM of the decode kernel; 0: occupancy maximum
   int fast = 1;              // settle shots 32 at a time before the per-shot path (GRAND_FAST)

@@ -103,7 +103,7 @@ class Engine:
         self.widths.append(h.shape[1])
         return cid.value
 
-    def set_tuning(self, light_log2=12, tile_k=4, search_ctas_per_sm=0):
+    def set_tuning(self, light_log2=10, tile_k=4, search_ctas_per_sm=0):
         rc = self.lib.grand_engine_set_tuning(self.h, light_log2, tile_k, search_ctas_per_sm)
         if rc != 0:
             raise ValueError("bad tuning")
