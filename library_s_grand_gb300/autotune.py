@@ -2,13 +2,14 @@
 
 Three knobs shape a launch and none of them changes a result:
   light_log2          largest per-iteration search (2^x candidates) finished by
-                      the triage warp itself instead of the search kernel;
+                      the warp that triages the shot instead of becoming a Job
+                      that every warp searches;
   tile_k              prefixes per lane in the masked colex tiles (weights 1-2,
                       and every weight when R > 256);
-  search_ctas_per_sm  resident CTAs of the persistent search kernel (0: the
-                      occupancy maximum).
-The tuner times a workload's device decode (CUDA events around the triage and
-search kernels) over a small grid, keeps the fastest setting on the engine and
+  search_ctas_per_sm  resident CTAs per SM of the persistent decode kernel (0:
+                      the occupancy maximum).
+The tuner times a workload's device decode (CUDA events around the control
+reset and the decode kernel) over a small grid, keeps the fastest setting on the engine and
 caches it in a JSON file keyed by the workload's name and the GPU.
 """
 from __future__ import annotations
@@ -52,8 +53,8 @@ def tune(engine, key, num_shots, d_records, d_results, stream, d_shot_code=0, d_
                                       d_offsets, use_graph=False)
             if rc != 0 or engine.sync_status(stream) != 0:
                 raise RuntimeError(f"decode failed under tuning {setting}")
-            tri, sea = engine.kernel_times(stream)
-            times.append(tri + sea)
+            reset_ms, decode_ms = engine.kernel_times(stream)
+            times.append(reset_ms + decode_ms)
         table.append((list(setting), float(np.median(times[1:]))))
     best = tuple(min(table, key=lambda t: t[1])[0])
     engine.set_tuning(*best)

@@ -201,7 +201,7 @@ struct alignas(128) Job {
   int n_it;
   int nseg;
   int final_iteration, final_tam; // outcome fields if nothing is found
-  int it_lo;                      // first iteration searched by the search kernel
+  int it_lo;                      // first iteration of the Job (searched in lookup tiles)
   unsigned long long tile_base;   // first tile of the Job (tiles numbered over all Jobs)
   unsigned long long ntiles;
   unsigned ready;                 // launch tag (epoch + 1) once the Job is fully written

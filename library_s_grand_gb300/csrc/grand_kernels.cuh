@@ -125,7 +125,7 @@ __device__ __forceinline__ void advance_front(const DevBatch &b, unsigned tag) {
 }
 
 // ---------------------------------------------------------------------------
-// Result writer shared by the light path and the search kernel (one warp).
+// Result writer shared by the per-shot path and the Job search (one warp).
 // ---------------------------------------------------------------------------
 struct Winner {
   int found;

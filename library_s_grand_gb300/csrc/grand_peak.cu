@@ -1,4 +1,4 @@
-// grand_peak.cu -- integer-ALU throughput probe (the search kernel's roofline).
+// grand_peak.cu -- integer-ALU throughput probe (the denominator of the search's roofline).
 //
 // The search is bound by 32-bit logic-op issue (LOP3 XOR/OR chains and IMNMX
 // minima), not by HBM or tensor cores.  This kernel issues independent lop3.b32

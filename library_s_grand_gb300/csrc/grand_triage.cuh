@@ -679,7 +679,7 @@ __device__ void triage_shot(const DevBatch &b, int slot, WarpArea &A, PlanState 
     tp = prof_lap(b, kProfShotCounts, tp);
 
     // ---- iterations in upstream order; the first one over the light budget
-    //      and everything after it go to the search kernel ---------------------
+    //      and everything after it become a Job that every warp searches -------
     const bool ml = MLK && cd.variant == kMl;
     const unsigned long long budget = 1ull << b.light_max_log2;
     Winner wn;

@@ -179,7 +179,7 @@ class Engine:
                 "longest_tile_draw_ns": out[30]}
 
     def batch_times(self):
-        """(h2d, triage, search, d2h) ms of the last host-buffer decode."""
+        """(h2d, control reset, decode kernel, d2h) ms of the last host-buffer decode."""
         v = [ctypes.c_float() for _ in range(4)]
         rc = self.lib.grand_engine_batch_times(self.h, *[ctypes.byref(x) for x in v])
         return tuple(x.value for x in v) if rc == 0 else None

@@ -1,4 +1,4 @@
-// Host build of the search kernels' warp-free index math (csrc/grand_device.cuh)
+// Host build of the searches' warp-free index math (csrc/grand_device.cuh)
 // checked against plain combinatorics: binomials, colex unranking (closed forms
 // and the table search), colex successors, lexicographic ranks, the FP32 cost
 // key, and whole run tiles (lane by lane) against a brute-force search in
@@ -214,7 +214,7 @@ int main() {
     for (int c = 0; c < tam; ++c) hc[c] = sketch(&cols[(size_t)c * nwp]);
     std::vector<float> llr(tam);
     for (auto &v : llr) v = (float)(1 + rng() % 6) * 0.25f;
-    // the search kernel's 8 prefixes per lane, or the triage warp's 4
+    // run tiles of 4 prefixes per lane (the light path's width) or 8
     const int KK = (rng() & 1) ? 8 : 4;
     const SegView sv{hc.data(), cols.data(), llr.data(), sketch(sw.data()), tam, w, KK,
                      nwp, nw, C(tam - 1, w - 1), 1000ull};

@@ -108,7 +108,7 @@ def test_uniform_errors(emulator, port, tmp_path, W, mode, thr, cap, light, pack
     prc, pres, pdec = port.css(O.UNIFORM, code.hx, code.hz, errors, None, O.Config(*cfg), "x")
     assert prc == 0
     _compare(res, dec, pres, pdec)
-    assert int(log.split()[3]) > 0 or light >= 12, log  # the search kernel had Jobs
+    assert int(log.split()[3]) > 0 or light >= 12, log  # the launch had Jobs
 
 
 @pytest.mark.parametrize("packed", [False, True])
@@ -127,7 +127,7 @@ def test_prob_syndromes(emulator, port, tmp_path, packed):
     prc, pres, pdec = port.css(O.PROB, code.hx, code.hz, None, syn, O.Config(*cfg), "x", phase)
     assert prc == 0
     _compare(res, dec, pres, pdec)
-    assert int(log.split()[3]) > 0, log  # the search kernel had Jobs
+    assert int(log.split()[3]) > 0, log  # the launch had Jobs
 
 
 @pytest.mark.parametrize("variant,packed", [("uniform", False), ("prob", False), ("ml", False),
@@ -153,7 +153,7 @@ def test_dem(emulator, port, tmp_path, variant, packed):
     assert np.array_equal(dlog, pdlog)
     if variant == "ml":
         assert np.array_equal(cost.view(np.uint32), np.asarray(pcost, np.float32).view(np.uint32))
-    assert int(out.split()[3]) > 0, out  # the search kernel had Jobs
+    assert int(out.split()[3]) > 0, out  # the launch had Jobs
 
 
 def test_wide_rows_and_weight_six(emulator, port, tmp_path):
@@ -241,7 +241,7 @@ def test_mixed_codes_in_one_batch(emulator, port, tmp_path, layout):
     # "ok N shots, J jobs, S slow": shots settled by the chunk step in either layout
     assert int(out.stdout.split()[5]) < N, out.stdout
     res = np.fromfile(d / "res.bin", dtype=capi.RESULT_DTYPE)
-    assert int(out.stdout.split()[3]) > 0, out.stdout  # the search kernel had Jobs
+    assert int(out.stdout.split()[3]) > 0, out.stdout  # the launch had Jobs
     got = np.empty(N, dtype=capi.RESULT_DTYPE)
     got[order] = res  # back to the per-code order
     _, p72, _ = port.css(O.UNIFORM, c72.hx, c72.hz, e72, None, O.Config(*cfg72), "x")
@@ -257,7 +257,7 @@ def test_largest_code_shapes(emulator, port, tmp_path):
     syndrome word) and 4000 columns (125 mask words per threshold iteration);
     syndromes of one or two columns, empty ones and random dense ones, with
     mode 1 and a cap that skip the dense shots' large active sets; three- and
-    four-column syndromes (beyond W = 2) become Jobs for the search kernel."""
+    four-column syndromes (beyond W = 2) become Jobs for the lookup search."""
     rng = np.random.default_rng(77)
     n, m = 1024, 4000
     hz = np.zeros((n, m), dtype=np.int32)
@@ -277,7 +277,7 @@ def test_largest_code_shapes(emulator, port, tmp_path):
     assert prc == 0
     _compare(res, dec, pres, pdec)
     assert int((pres["found"] == 1).sum()) >= 55
-    assert int(log.split()[3]) > 0, log  # the search kernel had Jobs
+    assert int(log.split()[3]) > 0, log  # the launch had Jobs
 
 
 def _slow(log):
