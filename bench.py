@@ -411,7 +411,7 @@ def run_ours(args):
 
 # DRAM bytes (read + write) of one decode_kernel launch on the headline batch, from an ncu
 # --set full capture (profiles/decode_kernel_prob_cc_bb144_16384.md).
-TRIAGE_TRAFFIC = 9.694976e6 + 768.0
+HEADLINE_TRAFFIC = 9.694976e6 + 768.0
 
 
 def hbm_peak():
@@ -432,7 +432,7 @@ def hbm_streaming(code, dec_ms):
     gbs = SHOTS * per_shot / (dec_ms * 1e-3) / 1e9
     return {"kernel": "decode_kernel", "achieved": gbs, "peak": peak, "unit": "GB/s",
             "frac": gbs / peak, "peak_source": src + " copy bandwidth (MEASURED_PEAKS.json)",
-            "algorithmic_bytes_per_launch": SHOTS * per_shot, "traffic": TRIAGE_TRAFFIC,
+            "algorithmic_bytes_per_launch": SHOTS * per_shot, "traffic": HEADLINE_TRAFFIC,
             "traffic_unit": "bytes per launch (ncu)", "decode_ms": dec_ms,
             "what": "bytes per launch: int32 error records (4m per shot) + 72-byte results"}
 
@@ -441,7 +441,7 @@ STRESS_SHOTS = 192
 SKETCH_OPS_PER_CANDIDATE = 1.5
 # DRAM bytes (read + write) of one decode_kernel launch on the 192 stress shots, from an
 # ncu --set full capture (profiles/decode_kernel_stress_bb144_w4.md), per shot.
-STRESS_TRAFFIC_PER_SHOT = (290048.0 + 8448.0) / 192
+STRESS_TRAFFIC_PER_SHOT = (317184.0 + 6656.0) / 192
 # The lookup search's bound per prefix probe: two shared-memory words (the last
 # element's sketch and one filter word) at 32 words per SM per clock.
 PROBE_WORDS = 2
