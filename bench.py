@@ -239,6 +239,36 @@ def stress_ops(code_h, syndromes, W):
     return cands, ops, prefixes
 
 
+def dem_stress_ops(h, detectors, W, cap):
+    """Exhaustive search work of unmatched DEM shots under the uniform search (mode -1),
+    iteration sets as upstream's DEM family (grand_decoder.cu:1542-1607): flagged-check
+    counts with the irregular offset (:376-416), and an iteration whose active set exceeds
+    the cap searches the last set within it instead (:1550-1554).  Returns (candidates,
+    ops, prefixes) as stress_ops."""
+    R = h.shape[0]
+    words = math.ceil(R / 32)
+    colw = h.sum(axis=0)
+    max_soma = int(colw.max())
+    sums = detectors.astype(np.int64) @ h.astype(np.int64) + np.where(colw > 0, max_soma - colw, 0)
+    sums[:, colw == 0] = 0
+    cands = ops = prefixes = 0
+    for s in sums:
+        tam_old = 0
+        for it in range(min(max_soma, 3)):
+            tam = int((s >= max_soma - it).sum())
+            if tam > cap:
+                tam = tam_old
+            else:
+                tam_old = tam
+            for w in range(1, min(W, 6) + 1):
+                if tam >= w:
+                    c = math.comb(tam, w)
+                    cands += c
+                    ops += c * (w + 1) * words
+                    prefixes += math.comb(tam - 1, w - 1)
+    return cands, ops, prefixes
+
+
 def run_ours(args):
     import torch
     from library_s_grand_gb300 import launch
@@ -383,6 +413,7 @@ def run_ours(args):
             extra["ml_dem"] = bench_ml(torch, lib, dev, sp, flush)
             extra["sampling"] = bench_sampling(torch, lib, dev, sp)
             extra["serving"] = bench_serving(lib)
+            extra["roofline_dem"] = dem_stress_roofline(torch, lib, dev, sp)
         cpu = cpu_baseline(seconds=args.cpu_seconds) if args.cpu_seconds > 0 else None
 
         out = {
@@ -511,6 +542,59 @@ def stress_roofline(torch, lib, dev, sp):
             "frac_probe_convention": prefixes / (search_ms * 1e-3) / probe_peak,
             "probe_convention": "one prefix probe = 2 shared-memory words (sketch, filter word); "
                                 "peak = SMs x 32 words/clock / 2 x 2.07 GHz"}
+
+
+STRESS_DEM_SHOTS = 8192
+
+
+def dem_stress_case(torch, lib, dev, n=STRESS_DEM_SHOTS):
+    """Engine + device buffers for the capped DEM stress (random detectors of the 120 x 720
+    DEM, grand_decode_cln, W = 3, cap 64)."""
+    from library_s_grand_gb300 import capi, workloads
+    from library_s_grand_gb300.engine import UNIFORM, Engine
+    wl = workloads.stress_dem(n)
+    eng = Engine(lib)
+    eng.add_dem(wl.dem.h, wl.dem.l, capi.GrandDecoderConfig(*wl.config), UNIFORM)
+    d_rec = torch.from_numpy(wl.records.ravel()).to(dev)
+    d_res = torch.empty(n * 72, dtype=torch.uint8, device=dev)
+    return wl, eng, d_rec, d_res
+
+
+def dem_stress_roofline(torch, lib, dev, sp):
+    """Decode kernel on the capped DEM stress, in the conventions of stress_roofline.  Each
+    shot's search is small (at most 43,744 candidates per iteration), so the figure covers
+    the whole per-shot pipeline (record, counts, planning, Job publication) as much as
+    the scan."""
+    from library_s_grand_gb300 import capi
+    n = STRESS_DEM_SHOTS
+    wl, eng, d_rec, d_res = dem_stress_case(torch, lib, dev, n)
+    cands, ops_fixed, prefixes = dem_stress_ops(wl.dem.h, wl.detectors, wl.W, wl.cap)
+    times = []
+    for rep in range(4):
+        eng.decode_device(n, d_rec.data_ptr(), d_res.data_ptr(), sp, use_graph=False)
+        if eng.sync_status(sp) != 0:
+            raise RuntimeError("DEM stress decode failed")
+        times.append(eng.kernel_times(sp)[1])
+    res = np.frombuffer(d_res.cpu().numpy().tobytes(), dtype=capi.RESULT_DTYPE)
+    assert int(res["found"].sum()) == 0
+    assert int(res["total_tested_combinations"].sum()) == cands, "count mismatch"
+    stats = eng.launch_stats(sp)
+    search_ms = float(np.median(times[1:]))
+    peak = eng.int_peak()
+    rate = cands / (search_ms * 1e-3)
+    words = math.ceil(wl.dem.n / 32)
+    return {"bound": "int_alu", "achieved": rate * SKETCH_OPS_PER_CANDIDATE / 1e9,
+            "peak": peak / 1e9, "unit": "Gop/s", "frac": rate * SKETCH_OPS_PER_CANDIDATE / peak,
+            "kernel": "decode_kernel",
+            "workload": f"{n} random-detector shots (Bernoulli 0.36) of the 120 x 720 DEM, "
+                        f"grand_decode_cln, W=3, cap 64, exhaustive ({cands} candidates)",
+            "ops_per_candidate": "1.5 (sketch XOR + half a 3-way min)",
+            "search_ms": search_ms, "candidates_per_s": rate, "shots_per_s": n / (search_ms * 1e-3),
+            "jobs": int(stats[2]), "lookup_tiles": int(stats[3]),
+            "frac_word_convention": rate * (words + 1) / peak,
+            "frac_fixed_convention": ops_fixed / (search_ms * 1e-3) / peak,
+            "prefix_probes": prefixes, "probes_per_s": prefixes / (search_ms * 1e-3),
+            "peak_source": "lop3.b32 issue rate measured on this GPU (grand_measure_int_peak)"}
 
 
 def _time_device(torch, eng, n, d_rec, d_res, sp, flush, steps, warmup, d_sc=0, d_off=0):
@@ -759,6 +843,9 @@ def run_case(args):
     if args.case == "stress":
         code, syn, eng, d_rec, d_res = stress_case(torch, lib, dev, args.case_shots or 48)
         n = len(syn)
+    elif args.case == "stress_dem":
+        wl, eng, d_rec, d_res = dem_stress_case(torch, lib, dev, args.case_shots or STRESS_DEM_SHOTS)
+        n = len(wl.detectors)
     else:
         tmp = tempfile.mkdtemp()
         phase = synth.write_phase_file(os.path.join(tmp, "phase.txt"), PHASE)
@@ -821,7 +908,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
-    ap.add_argument("--case", choices=["stress", "headline"], default=None,
+    ap.add_argument("--case", choices=["stress", "stress_dem", "headline"], default=None,
                     help="profiling mode: run one case --case-reps times, print kernel times")
     ap.add_argument("--case-reps", type=int, default=2)
     ap.add_argument("--case-shots", type=int, default=0)

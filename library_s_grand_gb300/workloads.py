@@ -14,7 +14,12 @@ tests decode, so that both work on the same shots:
 * ``bb_mix``         -- 100k syndrome records mixing BB[[72]], [[108]] (W = 3),
   [[144]] and [[288]] (W = 4) at p = 0.003, 25k each, shuffled with seed 0, cap 64;
 * ``stress_bb144``   -- random syndromes (Bernoulli 1/2) of BB[[144,12,12]], W = 4:
-  nothing matches, so every candidate of the three threshold iterations is tested.
+  nothing matches, so every candidate of the three threshold iterations is tested;
+* ``stress_dem``     -- random detectors (Bernoulli 0.36) of the ``ml_dem`` matrix,
+  grand_decode_cln, W = 3, cap 64: first active sets of ~40 columns (up to 64),
+  later iterations above the cap repeat that set (the DEM family's cap rule), and
+  nothing matches, so every candidate is tested (at most C(64,3) + C(64,2) + 64 =
+  43,744 per iteration).
 
 The upstream library builds its inputs with stim / qldpc (not available); these
 are numpy PCG64 stand-ins with the shapes and distributions of those workloads.
@@ -141,3 +146,16 @@ def stress_bb144(shots: int, seed: int = 1):
     code = synth.BB_CODES[144]()
     syn = (np.random.default_rng(seed).random((shots, code.n)) < 0.5).astype(np.int32)
     return code, syn
+
+
+STRESS_DEM_DENSITY = 0.36
+
+
+def stress_dem(shots: int, seed: int = 1) -> DemWorkload:
+    """Random detector records of the ml_dem matrix (logical flips all zero),
+    W = 3, cap 64, for a uniform (grand_decode_cln) search."""
+    dem = synth.random_dem(0)
+    rng = np.random.default_rng(seed)
+    det = (rng.random((shots, dem.n)) < STRESS_DEM_DENSITY).astype(np.int32)
+    log = np.zeros((shots, dem.l.shape[1]), dtype=np.int32)
+    return DemWorkload(dem, det, log, 3, 64)
