@@ -565,21 +565,30 @@ def dem_stress_roofline(torch, lib, dev, sp):
     shot's search is small (at most 43,744 candidates per iteration), so the figure covers
     the whole per-shot pipeline (record, counts, planning, Job publication) as much as
     the scan."""
-    from library_s_grand_gb300 import capi
+    from library_s_grand_gb300 import autotune, capi
     n = STRESS_DEM_SHOTS
     wl, eng, d_rec, d_res = dem_stress_case(torch, lib, dev, n)
     cands, ops_fixed, prefixes = dem_stress_ops(wl.dem.h, wl.detectors, wl.W, wl.cap)
-    times = []
-    for rep in range(4):
-        eng.decode_device(n, d_rec.data_ptr(), d_res.data_ptr(), sp, use_graph=False)
-        if eng.sync_status(sp) != 0:
-            raise RuntimeError("DEM stress decode failed")
-        times.append(eng.kernel_times(sp)[1])
-    res = np.frombuffer(d_res.cpu().numpy().tobytes(), dtype=capi.RESULT_DTYPE)
-    assert int(res["found"].sum()) == 0
-    assert int(res["total_tested_combinations"].sum()) == cands, "count mismatch"
-    stats = eng.launch_stats(sp)
-    search_ms = float(np.median(times[1:]))
+
+    def timed():
+        times = []
+        for rep in range(4):
+            eng.decode_device(n, d_rec.data_ptr(), d_res.data_ptr(), sp, use_graph=False)
+            if eng.sync_status(sp) != 0:
+                raise RuntimeError("DEM stress decode failed")
+            times.append(eng.kernel_times(sp)[1])
+        res = np.frombuffer(d_res.cpu().numpy().tobytes(), dtype=capi.RESULT_DTYPE)
+        assert int(res["found"].sum()) == 0
+        assert int(res["total_tested_combinations"].sum()) == cands, "count mismatch"
+        return float(np.median(times[1:])), eng.launch_stats(sp)
+
+    search_ms, stats = timed()
+    # the same shots with the light budget tuned for them (larger budgets keep these
+    # small searches in the warp that triages the shot instead of publishing Jobs)
+    best, table = autotune.tune(eng, "dem-stress", n, d_rec.data_ptr(), d_res.data_ptr(), sp,
+                                use_cache=False, grid=[(l, 4, 0) for l in (10, 12, 14, 16)])
+    tuned_ms, tuned_stats = timed()
+    eng.set_tuning()
     peak = eng.int_peak()
     rate = cands / (search_ms * 1e-3)
     words = math.ceil(wl.dem.n / 32)
@@ -594,7 +603,11 @@ def dem_stress_roofline(torch, lib, dev, sp):
             "frac_word_convention": rate * (words + 1) / peak,
             "frac_fixed_convention": ops_fixed / (search_ms * 1e-3) / peak,
             "prefix_probes": prefixes, "probes_per_s": prefixes / (search_ms * 1e-3),
-            "peak_source": "lop3.b32 issue rate measured on this GPU (grand_measure_int_peak)"}
+            "peak_source": "lop3.b32 issue rate measured on this GPU (grand_measure_int_peak)",
+            "tuned": {"light_log2": best[0], "search_ms": tuned_ms,
+                      "candidates_per_s": cands / (tuned_ms * 1e-3),
+                      "frac": cands / (tuned_ms * 1e-3) * SKETCH_OPS_PER_CANDIDATE / peak,
+                      "jobs": int(tuned_stats[2]), "table_ms": table}}
 
 
 def _time_device(torch, eng, n, d_rec, d_res, sp, flush, steps, warmup, d_sc=0, d_off=0):
