@@ -345,3 +345,53 @@ def test_dem_classification(emulator, port, tmp_path, fast):
         assert prc == 0
         _compare(res, dec, pres, pdec)
         assert np.array_equal(dlog, pdlog)
+
+
+def test_capped_dem_stress(emulator, port, tmp_path):
+    """Shots of the capped DEM stress (random detectors of the 120 x 720 DEM, W = 3,
+    cap 64): first active sets of up to 64 columns searched as Jobs, later
+    iterations above the cap repeating that set, nothing matched."""
+    from library_s_grand_gb300 import workloads
+    wl = workloads.stress_dem(6, seed=11)  # one shot's sets all exceed the cap: nothing searched
+    cfg = wl.config
+    res, dec, out, dlog, _ = _run(emulator, str(tmp_path), wl.dem.h, None, wl.detectors, False, 0,
+                                  cfg, [], 10, L=wl.dem.l, logicals=wl.logicals)
+    prc, pres, pdec, pdlog, _ = port.dem(O.UNIFORM, wl.dem.h, wl.dem.l, wl.detectors, wl.logicals,
+                                         O.Config(*cfg))
+    assert prc == 0
+    tot = pres["total_tested_combinations"]
+    assert int(pres["found"].sum()) == 0 and int(tot.max()) > 60000 and int(tot.min()) == 0
+    _compare(res, dec, pres, pdec)
+    assert np.array_equal(dlog, pdlog)
+    assert int(out.split()[3]) > 0, out  # the launch had Jobs
+
+
+@pytest.mark.parametrize("variant", ["uniform", "ml"])
+def test_dem_empty_and_duplicate_columns(emulator, port, tmp_path, variant):
+    """An irregular DEM with empty mechanisms (never active), duplicated columns
+    (equal sketches: the bucket walk and the exact test must keep the lower
+    rank) and columns of weight 1 beside weight 4 (the offset lifts them)."""
+    dem = synth.random_dem(13, detectors=36, mechanisms=150, logicals=4, col_weights=(1, 4),
+                           p_range=(5e-3, 3e-2))
+    h = dem.h.copy()
+    h[:, 7] = 0
+    h[:, 90] = 0
+    h[:, 31] = h[:, 30]
+    h[:, 120] = h[:, 5]
+    dem = synth.Dem(h, dem.l, dem.p, dem.llr)
+    det, log, _ = synth.dem_shots(dem, 120, seed=61)
+    cfg = (3, 256, 0, 40, 10, -1)
+    path, v, pv = None, 0, O.UNIFORM
+    if variant == "ml":
+        path, v, pv = synth.write_llr_file(str(tmp_path / "llr.txt"), dem.llr), 2, O.ML
+    d = tmp_path / "run"
+    d.mkdir()
+    res, dec, out, dlog, cost = _run(emulator, str(d), dem.h, None, det, False, v, cfg, [], 3,
+                                     L=dem.l, logicals=log, llr_path=path)
+    prc, pres, pdec, pdlog, pcost = port.dem(pv, dem.h, dem.l, det, log, O.Config(*cfg), path)
+    assert prc == 0
+    _compare(res, dec, pres, pdec)
+    assert np.array_equal(dlog, pdlog)
+    if variant == "ml":
+        assert np.array_equal(cost.view(np.uint32), np.asarray(pcost, np.float32).view(np.uint32))
+    assert int(out.split()[3]) > 0, out
