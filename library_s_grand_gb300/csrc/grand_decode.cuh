@@ -3,8 +3,9 @@
 // Every warp of the grid loops over whatever work the batch has left, in this
 // order of preference:
 //   1. classification chunks: 32 launch slots, one lane per shot; empty
-//      syndromes and weight-1 matches of a one-position first iteration are
-//      settled there, the other shots go to the slow queue (classify_chunk);
+//      syndromes and weight-1 matches of a one-position first iteration (a
+//      syndrome equal to a solo column, found by one sketch lookup) are settled
+//      there, the other shots go to the slow queue (classify_chunk);
 //   2. slow-queue shots: one warp per shot, the full threshold-iteration walk
 //      with the light search, publishing a Job for iterations over the light
 //      budget (triage_shot);
