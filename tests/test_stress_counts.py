@@ -42,6 +42,11 @@ def test_css_stress_counts(port):
     assert int(res["found"].sum()) == 0
     per_shot = [bench.stress_ops(code.hz, syn[i:i + 1], 4)[0] for i in range(len(syn))]
     assert per_shot == [int(v) for v in res["total_tested_combinations"]]
+    ref = _ref()
+    if ref is not None:
+        rc, rres = ref.css(O.UNIFORM, code.hx, code.hz, None, syn, cfg, "x")
+        assert rc == 0
+        assert [int(v) for v in rres["total_tested_combinations"]] == per_shot
 
 
 @pytest.mark.parametrize("cap", [0, 20, 64])
