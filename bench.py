@@ -12,12 +12,17 @@ Reported (one JSON line, rank 0):
              graph-replayed decode launches (one persistent kernel per batch), L2
              flushed between steps;
   e2e        shots/s through the upstream-compatible C ABI (grand_decode_prob_cc)
-             from host buffers, copies included;
+             from host buffers, the records' trip to the GPU and the results' trip
+             back included (read and written in place over NVLink-C2C where the
+             GPU can access pageable memory, else copied);
   roofline   the decode kernel on the stress input the integer roofline is
              defined on (random syndromes, W = 4, exhaustive enumeration):
              candidates at 1.5 integer ops each against the measured lop3 issue
              rate, and beside it the prefix probes the lookup search executes
              against the shared-memory bound of two words per probe;
+  roofline_dem  the same conventions on the capped DEM stress (random detectors
+             of the 120 x 720 DEM, W = 3, cap 64), at the default and at a tuned
+             light budget;
   cpu_baseline  the upstream CPU search algorithm (its C restatement in oracle/,
              or the upstream library itself where it was built) on all host cores.
 
